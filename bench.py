@@ -1,0 +1,430 @@
+"""Benchmark of the GB300 RMSD hot path; prints ONE JSON line (rank 0).
+
+Workload (default, 1 GPU): single-reference RMSD of 200,000 frames x 10,000
+atoms float32 (24 GB, axis-major on the device) to frame 0, not precentered:
+frame = R (reference + N(0, sigma^2)) + t with sigma log-uniform in
+[0.005, 0.5] nm, 1% exact rotated + translated copies; reference atoms
+uniform in a 4 nm cube.  Synthetic, seeded (there is no dataset).
+
+One step = one pass of md.rmsd's work (centre, trace, 3x3 inner product,
+FP64 QCP, refinement of near-identical frames) over all frames with the
+inputs resident in HBM; inputs are 24 GB >> L2 (129 MB), so no L2 flush is
+needed between steps.  `e2e` is the same metric through the drop-in
+md.rmsd (mdtraj_gb300.rmsd) with HOST numpy buffers: host->device copy of
+the coordinates, the kernels, device->host of the results and the
+reference's in-place centring side effect are all inside its timed region.
+
+--impl reference times mdtraj's own CPU kernels (compiled from the
+reference's sources by oracle/Makefile; the C restatement in oracle/ when
+those sources are absent) with all host threads on a bounded frame sample.
+
+Multi-GPU (torchrun, N > 1): frames are independent, so each rank processes
+its own shard of the same per-GPU size (weak scaling, no collective on the
+data path); timing is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOADS = {
+    # name: (n_frames, n_atoms, layout, sigma_lo, sigma_hi, exact_fraction)
+    "single_reference_200000x10000": (200_000, 10_000, 1, 0.005, 0.5, 0.01),
+    "single_reference_10000x1000": (10_000, 1_000, 0, 0.05, 0.05, 0.0),
+}
+DEFAULT_WORKLOAD = "single_reference_200000x10000"
+
+
+def measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": float(d["hbm_gbs"]), "src": "measured"}
+    return {"hbm_gbs": 6800.0, "src": "fallback"}
+
+
+def traffic_from_profiles(kernel: str, workload: str):
+    """DRAM bytes per launch of `kernel` from a committed ncu summary
+    (profiles/*.txt line: 'dram_bytes_per_launch <kernel> <workload> <bytes>')."""
+    for f in sorted((ROOT / "profiles").glob("*.txt")):
+        for line in f.read_text().splitlines():
+            m = re.match(r"dram_bytes_per_launch\s+(\S+)\s+(\S+)\s+([0-9.eE+]+)", line.strip())
+            if m and m.group(1) == kernel and m.group(2) == workload:
+                return float(m.group(3))
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks / throttle reasons during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        mx = max(r[1] for r in rows)
+        loaded = [r for r in rows if r[0] > 0.5 * mx] or rows
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in loaded for i, v in enumerate(r[2]) if v.lower().startswith("active")})
+        return {"sm_mhz": statistics.median(r[0] for r in loaded), "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def shard(n_frames: int, rank: int, world: int) -> tuple[int, int]:
+    """Weak scaling: every rank gets the full per-GPU workload; the global
+    frame index range of rank r is [r * n, (r + 1) * n)."""
+    return rank * n_frames, (rank + 1) * n_frames
+
+
+def max_over_ranks(value: float, world: int) -> float:
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([value], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline (reference implementation on the host cores)
+# ---------------------------------------------------------------------------
+
+
+def cpu_sample(n_atoms: int, n_sample: int, seed: int, sigma_lo: float, sigma_hi: float):
+    from mdtraj_gb300 import synth
+
+    rng = np.random.default_rng(seed)
+    sig = synth.log_uniform(rng, sigma_lo, sigma_hi, n_sample) if sigma_lo != sigma_hi else sigma_lo
+    ref, x = synth.single_reference_frames(n_sample, n_atoms, seed=seed, sigma=sig)
+    return ref, x
+
+
+def time_cpu_reference(n_atoms: int, budget_s: float, sigma_lo: float, sigma_hi: float) -> dict:
+    """Times md.rmsd's CPU path (reference kernels, OpenMP, all cores) on a
+    bounded sample; returns frames/s and a description."""
+    from oracle import cpu
+
+    impl = cpu.best_available()
+    n_sample = max(64, min(20_000, int(4e8 // max(n_atoms, 1) // 12)))  # <= ~400 MB sample
+    ref, x = cpu_sample(n_atoms, n_sample, 1234, sigma_lo, sigma_hi)
+    impl.md_rmsd(x[: min(256, n_sample)].copy(), ref.copy())  # warm up threads / pages
+    frames = 0
+    t_total = 0.0
+    reps = 0
+    while t_total < budget_s or reps < 2:
+        xs = x.copy()
+        rs = ref.copy()
+        t0 = time.perf_counter()
+        impl.md_rmsd(xs, rs)
+        t_total += time.perf_counter() - t0
+        frames += n_sample
+        reps += 1
+        if reps >= 200:
+            break
+    return {"value": frames / t_total, "unit": "frames/s", "cores": cpu.n_threads(), "kind": impl.kind,
+            "sample": f"{reps} x md.rmsd over {n_sample} frames x {n_atoms} atoms (same generator, "
+                      f"{t_total:.1f} s of CPU work, OpenMP threads={cpu.n_threads()})"}
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+
+
+def run_gpu(args) -> dict:
+    import torch
+
+    import mdtraj_gb300 as md
+    from mdtraj_gb300 import _device as D
+    from mdtraj_gb300 import _lib, synth
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    F, A, layout, s_lo, s_hi, exact = WORKLOADS[args.workload]
+    if args.frames:
+        F = args.frames
+    Ap = D.padded(A)
+    f0, f1 = shard(F, rank, world)
+    # ---- device-resident inputs
+    ref, x, sig = synth.device_single_reference(F, A, Ap, layout, seed=2024 + rank, device=dev,
+                                                sigma_lo=s_lo, sigma_hi=s_hi, exact_fraction=exact)
+    torch.cuda.synchronize()
+    dref = D.DeviceReference(ref, layout, centre=True, device=dev)
+    lib = _lib.lib
+    ws = D.empty_bytes(lib.gbrmsd_rmsd_workspace_bytes(F, A), dev)
+    out = torch.empty(F, dtype=torch.float32, device=dev)
+    stream = D.stream_handle()
+
+    def step():
+        _lib.check(lib.gbrmsd_rmsd_to_reference(x.data_ptr(), F, A, Ap, 3 * Ap, layout, _lib.MODE_CENTER,
+                                                dref.ws.data_ptr(), None, 0.0, -1, out.data_ptr(), None, None,
+                                                ws.data_ptr(), ws.numel(), stream))
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    _lib.check(lib.gbrmsd_workspace_status(ws.data_ptr(), stream))
+    lib.gbrmsd_profile_enable(args.steps)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        e0.record()
+        for _ in range(args.steps):
+            step()
+        e1.record()
+        torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    ms_total = e0.elapsed_time(e1)
+    kms = np.zeros(args.steps, dtype=np.float32)
+    nk = lib.gbrmsd_profile_read(kms.ctypes.data, args.steps)
+    lib.gbrmsd_profile_enable(0)
+    _lib.check(lib.gbrmsd_workspace_status(ws.data_ptr(), stream))
+    ms_step = max_over_ranks(ms_total / args.steps, world)
+    value = world * F / (ms_step / 1e3)
+
+    # ---- accuracy on the timed output (exact copies + random frames vs FP64)
+    acc = accuracy_check(x, ref, out, F, A, Ap, layout, sig, rank)
+
+    # ---- roofline of the streaming kernel
+    peaks = measured_peaks()
+    k_ms = float(np.mean(kms[:nk])) if nk > 0 else float("nan")
+    alg_bytes = 12.0 * A * F
+    achieved = alg_bytes / (k_ms / 1e3) / 1e9
+    traffic = traffic_from_profiles("stream_kernel", args.workload)
+    roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
+            "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": traffic,
+            "kernel": "stream_kernel", "kernel_ms": round(k_ms, 4),
+            "algorithmic_bytes_per_launch": alg_bytes, "peak_src": peaks["src"]}
+
+    del x
+    torch.cuda.empty_cache()
+    e2e = None
+    if rank == 0 and not args.skip_e2e:
+        e2e = run_e2e(args, F, A, s_lo, s_hi, exact, dev)
+    cpu_base = None
+    if rank == 0 and world == 1 and not args.skip_cpu:
+        cpu_base = time_cpu_reference(A, args.cpu_budget, s_lo, s_hi)
+
+    clocks = clk.summary()
+    return {
+        "metric": "rmsd_frames_per_s",
+        "value": round(value, 1),
+        "unit": "frames/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms_step, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded, generated on device)",
+        "config": {"workload": args.workload, "n_frames": F, "n_atoms": A,
+                   "layout": "axis-major" if layout == 1 else "atom-major", "precentered": False,
+                   "sigma_nm": [s_lo, s_hi], "exact_copy_fraction": exact,
+                   "l2": "inputs (%.1f GB) larger than L2; no flush" % (12.0 * Ap * F / 1e9),
+                   "parallelism": f"frame shards x{world}"},
+        "roofline": roof,
+        "cpu_baseline": cpu_base,
+        "e2e": e2e,
+        "gpu_launches": 3 * args.steps,
+        "clocks": clocks,
+        "accuracy": acc,
+    }
+
+
+def accuracy_check(x, ref, out, F, A, Ap, layout, sig, rank) -> dict:
+    """max/RMS |gpu - FP64 Kabsch| on every exact copy plus random frames."""
+    import torch
+
+    from oracle import fp64
+
+    rng = np.random.default_rng(7 + rank)
+    exact_idx = np.flatnonzero(sig == 0.0)
+    rand_idx = rng.choice(F, size=min(F, 2000 if A >= 5000 else 10000), replace=False)
+    idx = np.unique(np.concatenate([exact_idx, rand_idx, [0]]))[:6000]
+    sel = x[torch.from_numpy(idx).to(x.device)]
+    if layout == 1:
+        fr = sel[:, :, :A].transpose(1, 2).contiguous().cpu().numpy()
+    else:
+        fr = sel.view(len(idx), Ap, 3)[:, :A].contiguous().cpu().numpy()
+    want = fp64.kabsch_rmsd(fr, ref.cpu().numpy())
+    got = out[torch.from_numpy(idx).to(out.device)].cpu().numpy().astype(np.float64)
+    err = np.abs(got - want)
+    ex = np.isin(idx, exact_idx)
+    return {"checked_frames": int(len(idx)), "exact_copies": int(ex.sum()),
+            "max_err_nm": float(err.max()), "rms_err_nm": float(np.sqrt((err ** 2).mean())),
+            "max_err_exact_copies_nm": float(err[ex].max()) if ex.any() else None,
+            "oracle": "FP64 Kabsch/SVD (oracle/fp64.py)"}
+
+
+def run_e2e(args, F, A, s_lo, s_hi, exact, dev) -> dict:
+    """md.rmsd through the drop-in on host numpy buffers (atom-major, the
+    Trajectory.xyz layout).  Host data come from the device generator."""
+    import torch
+
+    import mdtraj_gb300 as md
+    from mdtraj_gb300 import _device as D
+    from mdtraj_gb300 import synth
+
+    Fe = F if args.e2e_frames is None else min(F, args.e2e_frames)
+    Ap = A  # host layout: unpadded (F, A, 3)
+    ref, xd, _ = synth.device_single_reference(Fe, A, D.padded(A), 0, seed=99, device=dev,
+                                               sigma_lo=s_lo, sigma_hi=s_hi, exact_fraction=exact)
+    host = np.empty((Fe, A, 3), dtype=np.float32)
+    host_t = torch.from_numpy(host)
+    step = 8192
+    for s in range(0, Fe, step):
+        e = min(Fe, s + step)
+        host_t[s:e].copy_(xd[s:e].view(e - s, D.padded(A), 3)[:, :A])
+    ref_h = ref.cpu().numpy()
+    del xd
+    torch.cuda.empty_cache()
+
+    class Obj:
+        def __init__(self, xyz):
+            self.xyz = xyz
+            self._rmsd_traces = None
+
+    target = Obj(host)
+    reference = Obj(ref_h[None].copy())
+    for _ in range(max(1, min(args.warmup, 2))):
+        md.rmsd(target, reference, 0)
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(args.e2e_steps):
+        t0 = time.perf_counter()
+        md.rmsd(target, reference, 0)
+        times.append(time.perf_counter() - t0)
+    t = float(np.mean(times))
+    return {"value": round(Fe / t, 1), "unit": "frames/s", "h2d_bytes_per_step": int(Fe * A * 12 + A * 12),
+            "d2h_bytes_per_step": int(Fe * 4 + Fe * 12), "ms_per_step": round(t * 1e3, 2),
+            "frames": Fe, "api": "mdtraj_gb300.rmsd(target, reference, 0) on host float32 arrays",
+            "steps": args.e2e_steps}
+
+
+def run_reference(args) -> dict:
+    rank, world, local = dist_env()
+    F, A, layout, s_lo, s_hi, exact = WORKLOADS[args.workload]
+    if rank != 0:
+        return None
+    base = time_cpu_reference(A, args.cpu_budget, s_lo, s_hi)
+    per_step_s = F / base["value"]
+    return {
+        "impl": "reference",
+        "metric": "rmsd_frames_per_s",
+        "value": round(base["value"], 1),
+        "unit": "frames/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(per_step_s * 1e3, 2),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded)",
+        "config": {"workload": args.workload, "n_frames": F, "n_atoms": A, "layout": "atom-major (host)",
+                   "precentered": False, "note": "each step timed on a bounded frame sample"},
+        "cpu_baseline": base,
+        "e2e": {"value": round(base["value"], 1), "unit": "frames/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
+    ap.add_argument("--frames", type=int, default=None, help="override n_frames (smaller runs)")
+    ap.add_argument("--e2e-frames", type=int, default=None)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU baseline work")
+    ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        res = run_reference(args)
+    else:
+        res = run_gpu(args)
+    rank = int(os.environ.get("RANK", "0"))
+    if rank == 0 and res is not None:
+        print(json.dumps(res), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,141 @@
+/*
+ * gbrmsd — C ABI of the GB300 (sm_103a) RMSD library behind mdtraj_gb300.
+ *
+ * Every pointer argument named x, ref, out_*, g_* or *_ws is a DEVICE pointer
+ * owned by the caller; the library allocates nothing on the device (scratch
+ * is passed in as a workspace sized by the *_workspace_bytes queries).
+ * `stream` is a cudaStream_t (NULL = legacy default stream).  All entry points
+ * are asynchronous with respect to the host unless stated otherwise, return
+ * GBRMSD_OK (0) on success and a negative GBRMSD_E_* code on failure, with a
+ * message available from gbrmsd_last_error() (thread-local).
+ *
+ * Coordinates are float32 nanometres in one of two padded layouts:
+ *   GBRMSD_ATOM_MAJOR  frame f, atom k, axis c at x[f*frame_stride + 3*k + c]
+ *   GBRMSD_AXIS_MAJOR  frame f, axis c, atom k at x[f*frame_stride + c*n_padded + k]
+ * with n_padded >= n_atoms, n_padded % 4 == 0, frame_stride % 4 == 0 and the
+ * base pointer 16-byte aligned (the bulk-copy engine moves 16-byte units).
+ * Padding atoms are ignored.  These mirror the reference's (n_real_atoms,
+ * n_padded_atoms, rowstride) conventions of mdtraj/rmsd/include/theobald_rmsd.h:13-18.
+ */
+#ifndef GBRMSD_H_
+#define GBRMSD_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBRMSD_OK 0
+#define GBRMSD_E_INVALID -1     /* bad argument (shape, alignment, mode) */
+#define GBRMSD_E_WORKSPACE -2   /* workspace missing or too small */
+#define GBRMSD_E_CUDA -3        /* CUDA runtime error (launch, copy) */
+#define GBRMSD_E_DEVICE -4      /* a kernel reported a device-side error */
+#define GBRMSD_E_UNSUPPORTED -5 /* device is not sm_103 / feature missing */
+
+#define GBRMSD_ATOM_MAJOR 0
+#define GBRMSD_AXIS_MAJOR 1
+
+/* Streaming modes (what the per-frame pass computes). */
+#define GBRMSD_MODE_CENTER 0      /* md.rmsd default: centre + trace + QCP      */
+#define GBRMSD_MODE_PRECENTERED 1 /* frames centred, traces supplied: QCP only  */
+#define GBRMSD_MODE_NOSUPERPOSE 2 /* md.rmsd(superpose=False)                   */
+
+/* Library identification. */
+int gbrmsd_version(void);
+const char* gbrmsd_last_error(void);
+
+/* 1 if the current device can run this library (sm_103), else 0. */
+int gbrmsd_device_supported(void);
+
+/* Device attributes of the current device, in this order: cc major, cc minor,
+ * SMs, max opt-in shared memory per block, pageable memory access, pageable
+ * access uses host page tables, concurrent managed access, host register
+ * supported, direct managed access from host, L2 bytes, SM clock kHz, memory
+ * clock kHz.  Writes min(n, count) values (-1 when unknown), returns count. */
+int gbrmsd_device_caps(int32_t* caps, int32_t n);
+
+/* ---- Reference preparation ------------------------------------------------
+ * Replaces inplace_center_and_trace_atom_major(ref, &g, 1, n)
+ * (mdtraj/rmsd/include/center.h:7-8, called at mdtraj/rmsd/_rmsd.pyx:213) for
+ * the reference frame, and additionally lays the reference out for the
+ * streaming kernels.  ref_xyz: raw (n_atoms, 3) atom-major frame on device.
+ * centre = 1: subtract the float centroid (double mean rounded to float, as the
+ * reference does); centre = 0: copy as is (precentered / no-superpose use).
+ */
+size_t gbrmsd_reference_workspace_bytes(int32_t n_atoms, int32_t n_padded);
+int gbrmsd_prepare_reference(const float* ref_xyz, int32_t n_atoms, int32_t n_padded,
+                             int32_t layout, int32_t centre, void* ref_ws, size_t ref_ws_bytes,
+                             void* stream);
+/* Copies the prepared reference's float trace and centroid to host memory
+ * (synchronises `stream`).  Either output may be NULL. */
+int gbrmsd_reference_info(const void* ref_ws, float* host_trace, float* host_centroid3,
+                          void* stream);
+
+/* ---- RMSD of every frame to one reference ---------------------------------
+ * mode GBRMSD_MODE_CENTER replaces the centre + prange(msd_atom_major) + sqrtf
+ * loop of md.rmsd (mdtraj/rmsd/_rmsd.pyx:211-224): frames are NOT modified;
+ * out_centroid (n_frames x 3 float, optional) receives the centroids the
+ * reference would subtract in place, out_trace (optional) the traces.
+ * mode GBRMSD_MODE_PRECENTERED replaces the prange loops over msd_axis_major
+ * / msd_atom_major of getMultipleRMSDs_axis_major / _atom_major
+ * (_rmsd.pyx:546-550, :606-609): g_target holds the per-frame traces and g_ref
+ * the reference trace; self_index = the frame whose storage is the reference
+ * (the reference's pointer-equality shortcut, theobald_rmsd_generic.h:22-23),
+ * or -1.
+ * mode GBRMSD_MODE_NOSUPERPOSE replaces msd_nosuperpose (_rmsd.pyx:762-793);
+ * the reference must then be prepared with centre = 0.
+ * ws: device workspace of at least gbrmsd_rmsd_workspace_bytes(...) bytes.
+ */
+size_t gbrmsd_rmsd_workspace_bytes(int64_t n_frames, int32_t n_atoms);
+int gbrmsd_rmsd_to_reference(const float* x, int64_t n_frames, int32_t n_atoms, int32_t n_padded,
+                             int64_t frame_stride, int32_t layout, int32_t mode,
+                             const void* ref_ws, const float* g_target, float g_ref,
+                             int64_t self_index, float* out_rmsd, float* out_centroid,
+                             float* out_trace, void* ws, size_t ws_bytes, void* stream);
+
+/* ---- In-place centring ------------------------------------------------------
+ * Replaces inplace_center_and_trace_atom_major (mdtraj/rmsd/include/center.h:7-8;
+ * src/center_generic.h:3-44) for whole trajectories on the device, i.e. the
+ * work of _center_inplace_atom_major (_rmsd.pyx:487-491) and
+ * Trajectory.center_coordinates (mdtraj/core/trajectory.py:2114-2137):
+ * centroid = double mean rounded to float, x -= centroid in float, trace =
+ * sum of float squares accumulated in extended precision, stored as float.
+ */
+int gbrmsd_center_inplace(float* x, int64_t n_frames, int32_t n_atoms, int32_t n_padded,
+                          int64_t frame_stride, int32_t layout, float* out_traces,
+                          float* out_centroids, void* ws, size_t ws_bytes, void* stream);
+
+/* Synchronises `stream` and returns GBRMSD_E_DEVICE if a kernel that used
+ * this workspace recorded a device-side error (e.g. a bounded wait expired),
+ * GBRMSD_OK otherwise.  The error word is cleared by the next call. */
+int gbrmsd_workspace_status(const void* ws, void* stream);
+
+/* Timing of the streaming kernel (the dominant kernel of
+ * gbrmsd_rmsd_to_reference) with CUDA events recorded on the caller's stream,
+ * for benchmarks.  gbrmsd_profile_enable(n) arms recording for the next n
+ * calls (0 disables; n <= 4096); gbrmsd_profile_read waits for the recorded
+ * calls, writes up to `capacity` kernel times in milliseconds, re-arms, and
+ * returns how many it wrote (negative on error).  Not thread-safe. */
+int gbrmsd_profile_enable(int32_t max_calls);
+int gbrmsd_profile_read(float* stream_kernel_ms, int32_t capacity);
+
+/* ---- Host<->device plumbing used by the drop-in ---------------------------
+ * Strided copy of n_rows rows of row_bytes bytes (cudaMemcpy2DAsync); kind:
+ * 1 = host->device, 2 = device->host, 3 = device->device. */
+int gbrmsd_copy_rows(void* dst, size_t dst_pitch, const void* src, size_t src_pitch,
+                     size_t row_bytes, size_t n_rows, int32_t kind, void* stream);
+
+/* Host-side replica of the reference's in-place centring side effect
+ * (src/center_generic.h:33-38: x -= (float)centroid, in float) on a HOST
+ * atom-major array, using centroids produced by gbrmsd_rmsd_to_reference.
+ * Multithreaded (n_threads <= 0: all hardware threads); synchronous. */
+int gbrmsd_host_subtract_centroids(float* x, int64_t n_frames, int32_t n_atoms, int64_t frame_stride,
+                                   const float* centroids, int32_t n_threads);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBRMSD_H_ */

@@ -1,0 +1,159 @@
+"""Device plumbing for the drop-in: torch owns device memory and streams,
+libgbrmsd does the work.  Nothing here computes RMSDs."""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import check, lib, ptr
+
+
+def require_device() -> torch.device:
+    """The CUDA device the drop-in runs on; raises if there is none (there is
+    no CPU implementation of the hot path)."""
+    if not torch.cuda.is_available():
+        raise RuntimeError(
+            "mdtraj_gb300 needs a CUDA device (GB300, sm_103); no CPU fallback is provided"
+        )
+    dev = torch.device("cuda", torch.cuda.current_device())
+    if not lib.gbrmsd_device_supported():
+        raise RuntimeError(
+            f"device {torch.cuda.get_device_name(dev)} is not sm_103: libgbrmsd.so is built for GB300 only"
+        )
+    return dev
+
+
+def stream_handle(stream: torch.cuda.Stream | None = None) -> int:
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return s.cuda_stream
+
+
+def padded(n_atoms: int) -> int:
+    """Atoms per frame in device memory: n_atoms rounded up to a multiple of 4
+    (the reference's padding convention for its aligned paths)."""
+    return (int(n_atoms) + 3) // 4 * 4
+
+
+def empty_bytes(nbytes: int, device) -> torch.Tensor:
+    return torch.empty(max(int(nbytes), 16), dtype=torch.uint8, device=device)
+
+
+def copy_rows(dst: int, dst_pitch: int, src: int, src_pitch: int, row_bytes: int, n_rows: int,
+              kind: int, stream: int) -> None:
+    check(lib.gbrmsd_copy_rows(dst, dst_pitch, src, src_pitch, row_bytes, n_rows, kind, stream))
+
+
+def frames_to_device(x: np.ndarray, layout: int, device, stream: int) -> tuple[torch.Tensor, int]:
+    """Copies host frames (F, A, 3) atom-major or (F, 3, A) axis-major into a
+    padded, 16-byte aligned device buffer.  Returns (buffer, n_padded)."""
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    F = x.shape[0]
+    if layout == _lib.ATOM_MAJOR:
+        A = x.shape[1]
+        Ap = padded(A)
+        buf = torch.empty((F, Ap * 3), dtype=torch.float32, device=device)
+        if F and A:
+            copy_rows(buf.data_ptr(), Ap * 12, x.ctypes.data, A * 12, A * 12, F, 1, stream)
+    else:
+        A = x.shape[2]
+        Ap = padded(A)
+        buf = torch.empty((F, 3, Ap), dtype=torch.float32, device=device)
+        if F and A:
+            copy_rows(buf.data_ptr(), Ap * 4, x.ctypes.data, A * 4, A * 4, F * 3, 1, stream)
+    return buf, Ap
+
+
+def frames_to_host(buf: torch.Tensor, out: np.ndarray, layout: int, n_atoms: int, n_padded: int,
+                   stream: int) -> None:
+    """Inverse of frames_to_device, writing into the existing host array."""
+    F = out.shape[0]
+    A = int(n_atoms)
+    if not F or not A:
+        return
+    if layout == _lib.ATOM_MAJOR:
+        copy_rows(out.ctypes.data, A * 12, buf.data_ptr(), n_padded * 12, A * 12, F, 2, stream)
+    else:
+        copy_rows(out.ctypes.data, A * 4, buf.data_ptr(), n_padded * 4, A * 4, F * 3, 2, stream)
+
+
+def to_host(t: torch.Tensor, stream: int) -> np.ndarray:
+    """Device tensor -> new host numpy array (synchronises the stream)."""
+    out = np.empty(tuple(t.shape), dtype=np.float32)
+    if out.size:
+        copy_rows(out.ctypes.data, out.nbytes, t.data_ptr(), out.nbytes, out.nbytes, 1, 2, stream)
+    torch.cuda.current_stream().synchronize()
+    return out
+
+
+class DeviceReference:
+    """A reference frame prepared on the device (centred or not), laid out
+    for the streaming kernels.  Reusable across calls."""
+
+    def __init__(self, ref_xyz: np.ndarray | torch.Tensor, layout: int, centre: bool, device=None):
+        device = device if device is not None else require_device()
+        stream = stream_handle()
+        if isinstance(ref_xyz, torch.Tensor):
+            raw = ref_xyz.to(device=device, dtype=torch.float32).contiguous().reshape(-1, 3)
+        else:
+            host = np.ascontiguousarray(ref_xyz, dtype=np.float32).reshape(-1, 3)
+            raw = torch.empty(host.shape, dtype=torch.float32, device=device)
+            if host.size:
+                copy_rows(raw.data_ptr(), host.nbytes, host.ctypes.data, host.nbytes, host.nbytes, 1, 1, stream)
+        self.n_atoms = int(raw.shape[0])
+        self.n_padded = padded(self.n_atoms)
+        self.layout = int(layout)
+        self.centred = bool(centre)
+        nbytes = lib.gbrmsd_reference_workspace_bytes(self.n_atoms, self.n_padded)
+        self.ws = empty_bytes(nbytes, device)
+        self._raw = raw  # keep alive until the preparation kernel has run
+        check(lib.gbrmsd_prepare_reference(raw.data_ptr() if raw.numel() else None, self.n_atoms,
+                                           self.n_padded, self.layout, int(centre),
+                                           self.ws.data_ptr(), self.ws.numel(), stream))
+
+    def info(self) -> tuple[float, np.ndarray]:
+        """(trace as float32, float32 centroid that was subtracted);
+        synchronises the current stream."""
+        stream = stream_handle()
+        g = _lib.C.c_float(0.0)
+        cen = np.zeros(3, dtype=np.float32)
+        check(lib.gbrmsd_reference_info(self.ws.data_ptr(), _lib.C.addressof(g), cen.ctypes.data, stream))
+        return float(np.float32(g.value)), cen
+
+
+def rmsd_to_reference(x: torch.Tensor, n_frames: int, n_atoms: int, n_padded: int, layout: int,
+                      mode: int, ref: DeviceReference, *, g_target: torch.Tensor | None = None,
+                      g_ref: float = 0.0, self_index: int = -1, out: torch.Tensor | None = None,
+                      centroid_out: torch.Tensor | None = None,
+                      trace_out: torch.Tensor | None = None) -> torch.Tensor:
+    """Device-resident RMSD of every frame of `x` to `ref` (see
+    gbrmsd_rmsd_to_reference) on torch's current stream, which also orders
+    the workspace's reuse.  Returns the float32 rmsd tensor."""
+    stream = stream_handle()
+    device = x.device
+    if out is None:
+        out = torch.empty(n_frames, dtype=torch.float32, device=device)
+    nbytes = lib.gbrmsd_rmsd_workspace_bytes(n_frames, n_atoms)
+    ws = empty_bytes(nbytes, device)
+    frame_stride = 3 * n_padded
+    check(lib.gbrmsd_rmsd_to_reference(
+        ptr(x), n_frames, n_atoms, n_padded, frame_stride, layout, mode, ref.ws.data_ptr(),
+        ptr(g_target), float(g_ref), int(self_index), ptr(out), ptr(centroid_out), ptr(trace_out),
+        ws.data_ptr(), ws.numel(), stream))
+    return out
+
+
+def center_inplace(x: torch.Tensor, n_frames: int, n_atoms: int, n_padded: int, layout: int,
+                   traces_out: torch.Tensor | None = None,
+                   centroid_out: torch.Tensor | None = None) -> torch.Tensor:
+    """Centres device frames in place on torch's current stream; returns the
+    float32 traces."""
+    stream = stream_handle()
+    device = x.device
+    if traces_out is None:
+        traces_out = torch.empty(n_frames, dtype=torch.float32, device=device)
+    nbytes = lib.gbrmsd_rmsd_workspace_bytes(n_frames, n_atoms)
+    ws = empty_bytes(nbytes, device)
+    check(lib.gbrmsd_center_inplace(ptr(x), n_frames, n_atoms, n_padded, 3 * n_padded, layout,
+                                    ptr(traces_out), ptr(centroid_out), ws.data_ptr(), ws.numel(), stream))
+    return traces_out

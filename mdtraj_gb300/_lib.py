@@ -1,0 +1,120 @@
+"""ctypes binding of libgbrmsd.so (declared in include/gbrmsd.h).
+
+The library is loaded at import.  There is no CPU fallback: if the shared
+library is missing the import fails with instructions to build it, and
+every entry point raises when its status code is non-zero.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+_LIB_PATH = Path(__file__).resolve().parent / "libgbrmsd.so"
+
+GBRMSD_OK = 0
+E_INVALID = -1
+E_WORKSPACE = -2
+E_CUDA = -3
+E_DEVICE = -4
+E_UNSUPPORTED = -5
+
+ATOM_MAJOR = 0
+AXIS_MAJOR = 1
+
+MODE_CENTER = 0
+MODE_PRECENTERED = 1
+MODE_NOSUPERPOSE = 2
+
+_vp = C.c_void_p
+_i32 = C.c_int32
+_i64 = C.c_int64
+_sz = C.c_size_t
+_f32 = C.c_float
+
+# name -> (restype, argtypes); must match include/gbrmsd.h
+SIGNATURES: dict[str, tuple] = {
+    "gbrmsd_version": (C.c_int, []),
+    "gbrmsd_last_error": (C.c_char_p, []),
+    "gbrmsd_device_supported": (C.c_int, []),
+    "gbrmsd_device_caps": (C.c_int, [_vp, _i32]),
+    "gbrmsd_reference_workspace_bytes": (_sz, [_i32, _i32]),
+    "gbrmsd_prepare_reference": (C.c_int, [_vp, _i32, _i32, _i32, _i32, _vp, _sz, _vp]),
+    "gbrmsd_reference_info": (C.c_int, [_vp, _vp, _vp, _vp]),
+    "gbrmsd_rmsd_workspace_bytes": (_sz, [_i64, _i32]),
+    "gbrmsd_rmsd_to_reference": (
+        C.c_int,
+        [_vp, _i64, _i32, _i32, _i64, _i32, _i32, _vp, _vp, _f32, _i64, _vp, _vp, _vp, _vp, _sz, _vp],
+    ),
+    "gbrmsd_center_inplace": (C.c_int, [_vp, _i64, _i32, _i32, _i64, _i32, _vp, _vp, _vp, _sz, _vp]),
+    "gbrmsd_workspace_status": (C.c_int, [_vp, _vp]),
+    "gbrmsd_profile_enable": (C.c_int, [_i32]),
+    "gbrmsd_profile_read": (C.c_int, [_vp, _i32]),
+    "gbrmsd_copy_rows": (C.c_int, [_vp, _sz, _vp, _sz, _sz, _sz, _i32, _vp]),
+    "gbrmsd_host_subtract_centroids": (C.c_int, [_vp, _i64, _i32, _i64, _vp, _i32]),
+}
+
+
+class GbrmsdError(RuntimeError):
+    """A libgbrmsd entry point returned a non-zero status."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(f"libgbrmsd error {code}: {message}")
+        self.code = code
+
+
+def _load() -> C.CDLL:
+    if not _LIB_PATH.exists():
+        raise ImportError(
+            f"{_LIB_PATH} is missing: build the CUDA library first "
+            "(python -c 'import __graft_entry__ as g; g.build()' or python mdtraj_gb300/build.py)"
+        )
+    lib = C.CDLL(str(_LIB_PATH))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
+lib = _load()
+
+
+def last_error() -> str:
+    msg = lib.gbrmsd_last_error()
+    return msg.decode() if msg else ""
+
+
+def check(rc: int) -> None:
+    """Raises on a non-zero status: ValueError for argument errors (the
+    reference raises ValueError for bad shapes), GbrmsdError otherwise."""
+    if rc == GBRMSD_OK:
+        return
+    msg = last_error()
+    if rc == E_INVALID:
+        raise ValueError(msg)
+    raise GbrmsdError(rc, msg)
+
+
+CAP_NAMES = ["cc_major", "cc_minor", "sms", "max_smem_optin", "pageable_memory_access",
+             "pageable_uses_host_page_tables", "concurrent_managed_access", "host_register_supported",
+             "direct_managed_access_from_host", "l2_bytes", "sm_clock_khz", "mem_clock_khz"]
+
+
+def device_caps() -> dict:
+    """Attributes of the current CUDA device (see gbrmsd_device_caps)."""
+    import numpy as np
+
+    buf = np.full(len(CAP_NAMES), -1, dtype=np.int32)
+    n = lib.gbrmsd_device_caps(buf.ctypes.data, len(CAP_NAMES))
+    if n < 0:
+        check(n)
+    return dict(zip(CAP_NAMES, buf.tolist()))
+
+
+def ptr(obj) -> int | None:
+    """Address of a torch tensor or numpy array (None for None)."""
+    if obj is None:
+        return None
+    if hasattr(obj, "data_ptr"):
+        return obj.data_ptr()
+    return obj.ctypes.data

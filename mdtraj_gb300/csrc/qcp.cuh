@@ -1,0 +1,160 @@
+// Quaternion characteristic polynomial (QCP) solve, FP64, one structure pair
+// per thread.
+//
+// Follows Theobald, Acta Cryst. A61:478 (2005) as used by mdtraj's
+// msdFromMandG (mdtraj/rmsd/src/theobald_rmsd.cpp:217-334): the 4x4 key
+// matrix K is built from the 3x3 inner-product matrix M = sum_k a_k b_k^T,
+// its characteristic polynomial is
+//     P(l) = l^4 + C2 l^2 + C1 l + C0,  C2 = -2 |M|_F^2, C1 = -8 det M, C0 = det K,
+// and msd = (G_a + G_b - 2 lambda_max) / n_atoms.  The reference forms the
+// coefficients in float32 and solves the quartic in closed form
+// (theobald_rmsd.cpp:81-193); here everything is FP64 and lambda_max is found
+// by Newton's method from the upper bound (G_a + G_b) / 2, which converges
+// monotonically from above (all roots lie below the start).
+#pragma once
+
+#include "common.cuh"
+
+namespace gb {
+
+struct Key4 {
+  double k00, k01, k02, k03, k11, k12, k13, k22, k23, k33;
+};
+
+// K(M) with M row-major, M[3*i + j] = sum_k a_k[i] * b_k[j]
+// (same entry layout as theobald_rmsd.cpp:227-236).
+__host__ __device__ __forceinline__ Key4 key_matrix(const double* m) {
+  Key4 k;
+  k.k00 = m[0] + m[4] + m[8];
+  k.k01 = m[5] - m[7];
+  k.k02 = m[6] - m[2];
+  k.k03 = m[1] - m[3];
+  k.k11 = m[0] - m[4] - m[8];
+  k.k12 = m[1] + m[3];
+  k.k13 = m[6] + m[2];
+  k.k22 = -m[0] + m[4] - m[8];
+  k.k23 = m[5] + m[7];
+  k.k33 = -m[0] - m[4] + m[8];
+  return k;
+}
+
+// Determinant of a symmetric 4x4 via complementary 2x2 minors of rows {0,1}
+// and {2,3}.
+__host__ __device__ __forceinline__ double det_sym4(const Key4& k) {
+  const double r0[4] = {k.k00, k.k01, k.k02, k.k03};
+  const double r1[4] = {k.k01, k.k11, k.k12, k.k13};
+  const double r2[4] = {k.k02, k.k12, k.k22, k.k23};
+  const double r3[4] = {k.k03, k.k13, k.k23, k.k33};
+  const double s01 = r0[0] * r1[1] - r0[1] * r1[0];
+  const double s02 = r0[0] * r1[2] - r0[2] * r1[0];
+  const double s03 = r0[0] * r1[3] - r0[3] * r1[0];
+  const double s12 = r0[1] * r1[2] - r0[2] * r1[1];
+  const double s13 = r0[1] * r1[3] - r0[3] * r1[1];
+  const double s23 = r0[2] * r1[3] - r0[3] * r1[2];
+  const double c01 = r2[0] * r3[1] - r2[1] * r3[0];
+  const double c02 = r2[0] * r3[2] - r2[2] * r3[0];
+  const double c03 = r2[0] * r3[3] - r2[3] * r3[0];
+  const double c12 = r2[1] * r3[2] - r2[2] * r3[1];
+  const double c13 = r2[1] * r3[3] - r2[3] * r3[1];
+  const double c23 = r2[2] * r3[3] - r2[3] * r3[2];
+  return s01 * c23 - s02 * c13 + s03 * c12 + s12 * c03 - s13 * c02 + s23 * c01;
+}
+
+__host__ __device__ __forceinline__ double det3(const double* m) {
+  return m[0] * (m[4] * m[8] - m[5] * m[7]) - m[1] * (m[3] * m[8] - m[5] * m[6]) +
+         m[2] * (m[3] * m[7] - m[4] * m[6]);
+}
+
+// Largest eigenvalue of K(M), by Newton on the characteristic quartic.
+// Returns the iteration count through *iters (capped at max_iter).
+__host__ __device__ __forceinline__ double qcp_lambda_max(const double* m, double ga, double gb,
+                                                          int* iters, int max_iter = 60) {
+  const Key4 k = key_matrix(m);
+  double c2 = 0.0;
+#pragma unroll
+  for (int i = 0; i < 9; ++i) c2 += m[i] * m[i];
+  c2 *= -2.0;
+  const double c1 = -8.0 * det3(m);
+  const double c0 = det_sym4(k);
+  double lam = 0.5 * (ga + gb);
+  int it = 0;
+  for (; it < max_iter; ++it) {
+    const double l2 = lam * lam;
+    const double b = (l2 + c2) * lam;
+    const double a = b + c1;
+    const double p = a * lam + c0;            // P(lam)
+    const double dp = 2.0 * l2 * lam + b + a; // P'(lam)
+    if (!(dp != 0.0)) break;
+    const double step = p / dp;
+    lam -= step;
+    if (!(fabs(step) > 1e-15 * fabs(lam))) {
+      ++it;
+      break;
+    }
+  }
+  if (iters) *iters = it;
+  return lam;
+}
+
+// Rotation R (row-major) minimising sum_k |R a_k - b_k|^2 for the given
+// lambda_max: the quaternion is the null vector of K - lambda I, taken as the
+// largest-norm row of its cofactor matrix (K is symmetric, so rows and columns
+// agree).  Returns false when K - lambda I has no well-defined null vector
+// (all cofactors vanish), in which case R is the identity.
+__host__ __device__ __forceinline__ bool qcp_rotation(const double* m, double lam, double* rot) {
+  Key4 k = key_matrix(m);
+  double a[4][4] = {{k.k00 - lam, k.k01, k.k02, k.k03},
+                    {k.k01, k.k11 - lam, k.k12, k.k13},
+                    {k.k02, k.k12, k.k22 - lam, k.k23},
+                    {k.k03, k.k13, k.k23, k.k33 - lam}};
+  double best[4] = {1.0, 0.0, 0.0, 0.0};
+  double best_n = 0.0;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    double q[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      // cofactor (i, j): determinant of a with row i and column j removed
+      double sub[9];
+      int idx = 0;
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        if (r == i) continue;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          if (c == j) continue;
+          sub[idx++] = a[r][c];
+        }
+      }
+      const double d = det3(sub);
+      q[j] = ((i + j) & 1) ? -d : d;
+    }
+    const double n = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
+    if (n > best_n) {
+      best_n = n;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) best[j] = q[j];
+    }
+  }
+  if (!(best_n > 0.0) || !(best_n < 1e300)) {
+    rot[0] = rot[4] = rot[8] = 1.0;
+    rot[1] = rot[2] = rot[3] = rot[5] = rot[6] = rot[7] = 0.0;
+    return false;
+  }
+  const double inv = 1.0 / sqrt(best_n);
+  const double w = best[0] * inv, x = best[1] * inv, y = best[2] * inv, z = best[3] * inv;
+  const double w2 = w * w, x2 = x * x, y2 = y * y, z2 = z * z;
+  const double xy = x * y, wz = w * z, zx = z * x, wy = w * y, yz = y * z, wx = w * x;
+  rot[0] = w2 + x2 - y2 - z2;
+  rot[1] = 2.0 * (xy - wz);
+  rot[2] = 2.0 * (zx + wy);
+  rot[3] = 2.0 * (xy + wz);
+  rot[4] = w2 - x2 + y2 - z2;
+  rot[5] = 2.0 * (yz - wx);
+  rot[6] = 2.0 * (zx - wy);
+  rot[7] = 2.0 * (yz + wx);
+  rot[8] = w2 - x2 - y2 + z2;
+  return true;
+}
+
+}  // namespace gb

@@ -1,0 +1,1083 @@
+// Single-reference streaming RMSD on GB300 (sm_103a).
+//
+// Work per call (all on one stream, no host synchronisation):
+//   1. stream_kernel   one pass over the frames.  Persistent CTAs (one per
+//                      SM), 8 warps each; every warp owns a ring of
+//                      shared-memory stages fed by 1-D bulk async copies
+//                      (cp.async.bulk + mbarrier, issued by lane 0) and
+//                      walks a static round-robin list of (frame, split)
+//                      units.  Per 4-atom quad a lane reads 3 x 128-bit
+//                      words of the frame and of the reference (the
+//                      reference lives in shared memory when it fits) and
+//                      accumulates, relative to a per-unit shift, the 3x3
+//                      inner product, the coordinate sum and the trace in
+//                      FP32 over one stage, then folds those into
+//                      error-free (TwoSum) float pairs.  A warp transpose
+//                      reduction turns the 13 sums into FP64 records.
+//   2. finish_kernel   one thread per frame: combines the split records in
+//                      FP64 (exact re-centring), solves QCP in FP64 (Newton
+//                      on the quartic) and writes rmsd / centroid / trace.
+//                      Frames whose msd is below what the one-pass sums can
+//                      resolve (near-identical structures) are queued.
+//   3. refine_kernel   one warp per queued frame: msd = sum |R (a - mu) -
+//                      b|^2 / n with the QCP rotation, which has no
+//                      cancellation as rmsd -> 0.
+//
+// Reference algorithm (CPU): mdtraj/rmsd/_rmsd.pyx:211-224 (centre, then
+// msd_atom_major per frame), src/center_generic.h:3-44 (centring),
+// src/theobald_rmsd_generic.h:7-119 (3x3 inner products),
+// src/theobald_rmsd.cpp:217-334 (QCP).
+#include <math.h>
+
+#include "capi_internal.h"
+#include "common.cuh"
+#include "qcp.cuh"
+#include "stream.cuh"
+
+namespace gb {
+
+namespace {
+
+constexpr int HDR_BYTES = 256;  // workspace header: err word, refine count
+
+struct WsHeader {
+  int err;
+  int refine_count;
+};
+
+// ---------------------------------------------------------------------------
+// Reference preparation (one CTA)
+// ---------------------------------------------------------------------------
+
+constexpr int PREP_THREADS = 1024;
+
+__device__ double block_sum_d(double v, double* red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  v = warp_sum_d(v);
+  __syncthreads();
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (warp == 0) {
+    t = (lane < (int)(blockDim.x >> 5)) ? red[lane] : 0.0;
+    t = warp_sum_d(t);
+    if (lane == 0) red[0] = t;
+  }
+  __syncthreads();
+  t = red[0];
+  __syncthreads();
+  return t;
+}
+
+__global__ void __launch_bounds__(PREP_THREADS) ref_prepare_kernel(
+    const float* __restrict__ raw, int32_t A, int32_t Ap, int32_t layout, int32_t centre,
+    float* __restrict__ out, RefInfo* __restrict__ info, double* __restrict__ prefix) {
+  __shared__ double red[32];
+  __shared__ double part[PREP_THREADS * 3];
+  const int tid = threadIdx.x;
+  // 1. centroid: double accumulation, rounded to float (center_generic.h:19-29)
+  float mu[3] = {0.f, 0.f, 0.f};
+  if (centre) {
+    double s[3] = {0.0, 0.0, 0.0};
+    for (int k = tid; k < A; k += blockDim.x)
+      for (int c = 0; c < 3; ++c) s[c] += (double)raw[3 * k + c];
+    for (int c = 0; c < 3; ++c) {
+      const double t = block_sum_d(s[c], red);
+      mu[c] = (float)(t / (double)A);
+    }
+  }
+  // 2. centred (float subtraction) reference in the requested layout
+  double g = 0.0, sb[3] = {0.0, 0.0, 0.0};
+  for (int k = tid; k < Ap; k += blockDim.x) {
+    for (int c = 0; c < 3; ++c) {
+      float v = 0.f;
+      if (k < A) v = __fsub_rn(raw[3 * k + c], mu[c]);
+      if (layout == ATOM_MAJOR)
+        out[3 * (size_t)k + c] = v;
+      else
+        out[(size_t)c * Ap + k] = v;
+      g += (double)v * (double)v;
+      sb[c] += (double)v;
+    }
+  }
+  g = block_sum_d(g, red);
+  for (int c = 0; c < 3; ++c) sb[c] = block_sum_d(sb[c], red);
+  // 3. prefix sums over quads (for splitting frames across warps)
+  const int Q = (A + 3) >> 2;
+  const int per = (Q + PREP_THREADS - 1) / PREP_THREADS;
+  const int q_lo = min(Q, tid * per), q_hi = min(Q, q_lo + per);
+  double loc[3] = {0.0, 0.0, 0.0};
+  for (int q = q_lo; q < q_hi; ++q)
+    for (int t = 0; t < 4; ++t) {
+      const int k = 4 * q + t;
+      if (k < A)
+        for (int c = 0; c < 3; ++c) loc[c] += (double)__fsub_rn(raw[3 * k + c], mu[c]);
+    }
+  for (int c = 0; c < 3; ++c) part[3 * tid + c] = loc[c];
+  __syncthreads();
+  if (tid == 0) {
+    double run[3] = {0.0, 0.0, 0.0};
+    for (int t = 0; t < PREP_THREADS; ++t)
+      for (int c = 0; c < 3; ++c) {
+        const double v = part[3 * t + c];
+        part[3 * t + c] = run[c];
+        run[c] += v;
+      }
+  }
+  __syncthreads();
+  double run[3] = {part[3 * tid], part[3 * tid + 1], part[3 * tid + 2]};
+  for (int q = q_lo; q < q_hi; ++q) {
+    for (int c = 0; c < 3; ++c) prefix[3 * (size_t)q + c] = run[c];
+    for (int t = 0; t < 4; ++t) {
+      const int k = 4 * q + t;
+      if (k < A)
+        for (int c = 0; c < 3; ++c) run[c] += (double)__fsub_rn(raw[3 * k + c], mu[c]);
+    }
+  }
+  if (q_lo < q_hi && q_hi == Q)
+    for (int c = 0; c < 3; ++c) prefix[3 * (size_t)Q + c] = run[c];
+  if (Q == 0 && tid == 0)
+    for (int c = 0; c < 3; ++c) prefix[c] = 0.0;
+  if (tid == 0) {
+    info->g = g;
+    for (int c = 0; c < 3; ++c) {
+      info->sum[c] = sb[c];
+      info->centroid[c] = mu[c];
+    }
+    info->n_atoms = A;
+    info->n_padded = Ap;
+    info->layout = layout;
+    info->centred = centre;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Streaming pass
+// ---------------------------------------------------------------------------
+
+struct Cursor {
+  int64_t unit;
+  int64_t frame;
+  int32_t q0, q1;  // quad range of the unit
+  int32_t c;       // chunk index within the unit
+};
+
+template <int CQ>
+__device__ __forceinline__ void cursor_unit(Cursor& cur, int64_t u, int32_t S, int32_t Q) {
+  cur.unit = u;
+  cur.frame = u / S;
+  const int32_t s = (int32_t)(u - cur.frame * S);
+  cur.q0 = (int32_t)(((int64_t)s * Q) / S);
+  cur.q1 = (int32_t)(((int64_t)(s + 1) * Q) / S);
+  cur.c = 0;
+}
+
+// Advances to the next chunk; returns true when a new unit starts.
+template <int CQ>
+__device__ __forceinline__ bool cursor_next(Cursor& cur, int64_t W, int32_t S, int32_t Q) {
+  cur.c += 1;
+  if (cur.q0 + cur.c * CQ >= cur.q1) {
+    cursor_unit<CQ>(cur, cur.unit + W, S, Q);
+    return true;
+  }
+  return false;
+}
+
+template <int LAYOUT, int CQ>
+__device__ __forceinline__ void issue_chunk(const StreamArgs& p, const Cursor& cur,
+                                            unsigned char* stage, uint64_t* bar) {
+  const int32_t qb = cur.q0 + cur.c * CQ;
+  const int32_t nq = min(CQ, cur.q1 - qb);
+  const float* fbase = p.x + cur.frame * p.frame_stride;
+  mbar_arrive_expect_tx(bar, (uint32_t)nq * 48u);
+  if (LAYOUT == ATOM_MAJOR) {
+    bulk_g2s(stage, fbase + (size_t)qb * 12, (uint32_t)nq * 48u, bar);
+  } else {
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+      bulk_g2s(stage + r * CQ * 16, fbase + (size_t)r * p.n_padded + (size_t)qb * 4,
+               (uint32_t)nq * 16u, bar);
+  }
+}
+
+// Loads quad i of a stage (or of the reference) as x[4], y[4], z[4].
+template <int LAYOUT, int CQ>
+__device__ __forceinline__ void load_stage_quad(const float* st, int i, float (&x)[4], float (&y)[4],
+                                                float (&z)[4]) {
+  if (LAYOUT == ATOM_MAJOR) {
+    const float4 t0 = lds4(st + 12 * i), t1 = lds4(st + 12 * i + 4), t2 = lds4(st + 12 * i + 8);
+    x[0] = t0.x; y[0] = t0.y; z[0] = t0.z; x[1] = t0.w;
+    y[1] = t1.x; z[1] = t1.y; x[2] = t1.z; y[2] = t1.w;
+    z[2] = t2.x; x[3] = t2.y; y[3] = t2.z; z[3] = t2.w;
+  } else {
+    const float4 tx = lds4(st + 4 * i), ty = lds4(st + CQ * 4 + 4 * i),
+                 tz = lds4(st + 2 * CQ * 4 + 4 * i);
+    x[0] = tx.x; x[1] = tx.y; x[2] = tx.z; x[3] = tx.w;
+    y[0] = ty.x; y[1] = ty.y; y[2] = ty.z; y[3] = ty.w;
+    z[0] = tz.x; z[1] = tz.y; z[2] = tz.z; z[3] = tz.w;
+  }
+}
+
+template <int LAYOUT, bool SMEM>
+__device__ __forceinline__ void load_ref_quad(const float* ref, int32_t Ap, int32_t gq, float (&x)[4],
+                                              float (&y)[4], float (&z)[4]) {
+  float4 t0, t1, t2;
+  if (LAYOUT == ATOM_MAJOR) {
+    const float* q = ref + (size_t)gq * 12;
+    if (SMEM) { t0 = lds4(q); t1 = lds4(q + 4); t2 = lds4(q + 8); }
+    else { t0 = ldg4(q); t1 = ldg4(q + 4); t2 = ldg4(q + 8); }
+    x[0] = t0.x; y[0] = t0.y; z[0] = t0.z; x[1] = t0.w;
+    y[1] = t1.x; z[1] = t1.y; x[2] = t1.z; y[2] = t1.w;
+    z[2] = t2.x; x[3] = t2.y; y[3] = t2.z; z[3] = t2.w;
+  } else {
+    const float* q = ref + (size_t)gq * 4;
+    if (SMEM) { t0 = lds4(q); t1 = lds4(q + Ap); t2 = lds4(q + 2 * (size_t)Ap); }
+    else { t0 = ldg4(q); t1 = ldg4(q + Ap); t2 = ldg4(q + 2 * (size_t)Ap); }
+    x[0] = t0.x; x[1] = t0.y; x[2] = t0.z; x[3] = t0.w;
+    y[0] = t1.x; y[1] = t1.y; y[2] = t1.z; y[3] = t1.w;
+    z[0] = t2.x; z[1] = t2.y; z[2] = t2.z; z[3] = t2.w;
+  }
+}
+
+// Number of level-1 sums per mode.
+template <int MODE>
+struct NSums {
+  static constexpr int value = MODE == MODE_CENTER ? 13 : MODE == MODE_PRECENTERED ? 9 : MODE == MODE_NOSUPERPOSE ? 1 : 3;
+};
+
+template <int LAYOUT, int MODE, int CQ, int NSTAGE, bool REF_SMEM>
+__global__ void __launch_bounds__(kWarps * 32, 1) stream_kernel(const StreamArgs p) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  constexpr int STAGE_BYTES = CQ * 48;
+  constexpr int NV = NSums<MODE>::value;
+  constexpr bool USE_REF = MODE != MODE_TRACE;
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int32_t A = p.n_atoms;
+  const int32_t Ap = p.n_padded;
+  const int32_t Q = (A + 3) >> 2;
+  const int32_t S = p.splits;
+  const size_t ref_al = REF_SMEM ? align_up((size_t)Ap * 12, 128) : 0;
+  float* sref = reinterpret_cast<float*>(smem);
+  unsigned char* stages = smem + ref_al + (size_t)warp * NSTAGE * STAGE_BYTES;
+  uint64_t* bars =
+      reinterpret_cast<uint64_t*>(smem + ref_al + (size_t)kWarps * NSTAGE * STAGE_BYTES) + warp * NSTAGE;
+
+  if (REF_SMEM && USE_REF) {
+    const float4* src = reinterpret_cast<const float4*>(p.ref);
+    float4* dst = reinterpret_cast<float4*>(sref);
+    const int n4 = Ap * 3 / 4;
+    for (int i = threadIdx.x; i < n4; i += blockDim.x) dst[i] = src[i];
+  }
+  if (lane == 0) {
+    for (int s = 0; s < NSTAGE; ++s) mbar_init(&bars[s], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  const float* rbase = REF_SMEM ? sref : p.ref;
+
+  const int64_t n_units = p.n_frames * S;
+  const int64_t W = (int64_t)gridDim.x * kWarps;
+  const int64_t gw = (int64_t)blockIdx.x * kWarps + warp;
+
+  // Producer cursor runs NSTAGE chunks ahead of the consumer cursor.
+  Cursor pc, cc;
+  cursor_unit<CQ>(pc, gw, S, Q);
+  cursor_unit<CQ>(cc, gw, S, Q);
+  int64_t issued = 0, consumed = 0;
+#pragma unroll 1
+  for (int s = 0; s < NSTAGE; ++s) {
+    if (pc.unit < n_units) {
+      if (lane == 0) issue_chunk<LAYOUT, CQ>(p, pc, stages + s * STAGE_BYTES, &bars[s]);
+      cursor_next<CQ>(pc, W, S, Q);
+      ++issued;
+    }
+  }
+  __syncwarp();
+
+  uint32_t phases = 0;
+  int slot = 0;
+  bool failed = false;
+  CF acc2[NV];
+  float shift[3] = {0.f, 0.f, 0.f};
+
+#pragma unroll 1
+  while (cc.unit < n_units) {
+    const bool unit_start = (cc.c == 0);
+    if (unit_start) {
+#pragma unroll
+      for (int j = 0; j < NV; ++j) acc2[j] = cf_zero();
+    }
+    const int32_t qb = cc.q0 + cc.c * CQ;
+    const int32_t nq = min(CQ, cc.q1 - qb);
+    if (!mbar_wait_bounded(&bars[slot], (phases >> slot) & 1u, p.err)) {
+      failed = true;
+      break;
+    }
+    phases ^= 1u << slot;
+    ++consumed;
+    const float* st = reinterpret_cast<const float*>(stages + slot * STAGE_BYTES);
+
+    if (MODE == MODE_CENTER && unit_start) {
+      // Shift = mean of the first atoms of the unit (lane's first quad).
+      float sx = 0.f, sy = 0.f, sz = 0.f, cnt = 0.f;
+      if (lane < nq) {
+        float x[4], y[4], z[4];
+        load_stage_quad<LAYOUT, CQ>(st, lane, x, y, z);
+        const int nv = A - 4 * (qb + lane);
+#pragma unroll
+        for (int t = 0; t < 4; ++t)
+          if (t < nv) { sx += x[t]; sy += y[t]; sz += z[t]; cnt += 1.f; }
+      }
+      sx = warp_sum(sx); sy = warp_sum(sy); sz = warp_sum(sz); cnt = warp_sum(cnt);
+      shift[0] = sx / cnt; shift[1] = sy / cnt; shift[2] = sz / cnt;
+    }
+
+    float acc1[NV];
+#pragma unroll
+    for (int j = 0; j < NV; ++j) acc1[j] = 0.f;
+
+#pragma unroll
+    for (int kq = 0; kq < CQ / 32; ++kq) {
+      const int i = lane + 32 * kq;
+      if (i < nq) {
+        const int32_t gq = qb + i;
+        const int nv = A - 4 * gq;  // >= 1 by construction
+        float ax[4], ay[4], az[4];
+        load_stage_quad<LAYOUT, CQ>(st, i, ax, ay, az);
+        float bx[4] = {0.f, 0.f, 0.f, 0.f}, by[4] = {0.f, 0.f, 0.f, 0.f}, bz[4] = {0.f, 0.f, 0.f, 0.f};
+        if constexpr (USE_REF) load_ref_quad<LAYOUT, REF_SMEM>(rbase, Ap, gq, bx, by, bz);
+        if constexpr (MODE == MODE_TRACE) {
+          // exact centroid: compensated per-atom sums of the raw coordinates
+#pragma unroll
+          for (int t = 0; t < 4; ++t)
+            if (t < nv) { cf_add(acc2[0], ax[t]); cf_add(acc2[1], ay[t]); cf_add(acc2[2], az[t]); }
+          continue;
+        }
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+          const bool ok = t < nv;
+          float dx, dy, dz;
+          if constexpr (MODE == MODE_CENTER) {
+            dx = ax[t] - shift[0]; dy = ay[t] - shift[1]; dz = az[t] - shift[2];
+          } else if constexpr (MODE == MODE_NOSUPERPOSE) {
+            dx = ax[t] - bx[t]; dy = ay[t] - by[t]; dz = az[t] - bz[t];
+          } else {
+            dx = ax[t]; dy = ay[t]; dz = az[t];
+          }
+          if (!ok) { dx = 0.f; dy = 0.f; dz = 0.f; }
+          if constexpr (MODE == MODE_NOSUPERPOSE) {
+            acc1[0] = fmaf(dx, dx, acc1[0]);
+            acc1[0] = fmaf(dy, dy, acc1[0]);
+            acc1[0] = fmaf(dz, dz, acc1[0]);
+          } else {
+            acc1[0] = fmaf(dx, bx[t], acc1[0]);
+            acc1[1] = fmaf(dx, by[t], acc1[1]);
+            acc1[2] = fmaf(dx, bz[t], acc1[2]);
+            acc1[3] = fmaf(dy, bx[t], acc1[3]);
+            acc1[4] = fmaf(dy, by[t], acc1[4]);
+            acc1[5] = fmaf(dy, bz[t], acc1[5]);
+            acc1[6] = fmaf(dz, bx[t], acc1[6]);
+            acc1[7] = fmaf(dz, by[t], acc1[7]);
+            acc1[8] = fmaf(dz, bz[t], acc1[8]);
+            if constexpr (MODE == MODE_CENTER) {
+              acc1[9] += dx;
+              acc1[10] += dy;
+              acc1[11] += dz;
+              float gg = acc1[12];
+              gg = fmaf(dx, dx, gg);
+              gg = fmaf(dy, dy, gg);
+              gg = fmaf(dz, dz, gg);
+              acc1[12] = gg;
+            }
+          }
+        }
+      }
+    }
+    if constexpr (MODE != MODE_TRACE) {
+#pragma unroll
+      for (int j = 0; j < NV; ++j) cf_add(acc2[j], acc1[j]);
+    }
+
+    // Release the stage and refill it with the chunk NSTAGE ahead.
+    __syncwarp();
+    if (pc.unit < n_units) {
+      if (lane == 0) {
+        fence_proxy_async_smem();
+        issue_chunk<LAYOUT, CQ>(p, pc, stages + slot * STAGE_BYTES, &bars[slot]);
+      }
+      cursor_next<CQ>(pc, W, S, Q);
+      ++issued;
+    }
+    slot = (slot + 1 == NSTAGE) ? 0 : slot + 1;
+
+    const int64_t unit = cc.unit;
+    const bool unit_end = cursor_next<CQ>(cc, W, S, Q);
+    if (unit_end) {
+      double* rec = p.sums + unit * SUMS_STRIDE;
+      if constexpr (NV == 1) {
+        CF v = acc2[0];
+#pragma unroll
+        for (int m = 16; m >= 1; m >>= 1) {
+          CF o;
+          o.hi = __shfl_xor_sync(FULL_MASK, v.hi, m);
+          o.lo = __shfl_xor_sync(FULL_MASK, v.lo, m);
+          v = cf_add2(v, o);
+        }
+        if (lane == 0) rec[12] = cf_to_double(v);
+      } else if constexpr (NV == 3) {
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          CF v = acc2[j];
+#pragma unroll
+          for (int m = 16; m >= 1; m >>= 1) {
+            CF o;
+            o.hi = __shfl_xor_sync(FULL_MASK, v.hi, m);
+            o.lo = __shfl_xor_sync(FULL_MASK, v.lo, m);
+            v = cf_add2(v, o);
+          }
+          if (lane == 0) rec[9 + j] = cf_to_double(v);
+        }
+      } else {
+        CF v[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) v[j] = (j < NV) ? acc2[j < NV ? j : 0] : cf_zero();
+        warp_xpose_reduce16(v, lane);
+        const int idx = lane >> 1;
+        if ((lane & 1) == 0 && idx < NV) rec[idx] = cf_to_double(v[0]);
+      }
+      if (lane == 0 && MODE == MODE_CENTER) {
+        rec[16] = shift[0];
+        rec[17] = shift[1];
+        rec[18] = shift[2];
+      }
+    }
+  }
+
+  if (failed) {
+    // Drain this warp's copies still in flight (bounded), then leave.
+    while (consumed < issued) {
+      if (!mbar_wait_bounded(&bars[slot], (phases >> slot) & 1u, nullptr)) break;
+      phases ^= 1u << slot;
+      slot = (slot + 1 == NSTAGE) ? 0 : slot + 1;
+      ++consumed;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// QCP finish: one thread per frame
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(256) finish_kernel(const FinishArgs a) {
+  const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= a.n_frames) return;
+  const int32_t A = a.n_atoms;
+  const int32_t S = a.splits;
+  const int32_t Q = (A + 3) >> 2;
+  const double* base = a.sums + f * (int64_t)S * SUMS_STRIDE;
+  const double dA = (double)A;
+
+  if (a.mode == MODE_NOSUPERPOSE) {
+    double g = 0.0;
+    for (int j = 0; j < S; ++j) g += base[j * SUMS_STRIDE + 12];
+    double msd = g / dA;
+    if (!(msd > 0.0)) msd = 0.0;
+    a.out_rmsd[f] = (float)sqrt(msd);
+    return;
+  }
+  if (a.mode == MODE_TRACE) {
+    for (int c = 0; c < 3; ++c) {
+      double s = 0.0;
+      for (int j = 0; j < S; ++j) s += base[j * SUMS_STRIDE + 9 + c];
+      a.out_centroid[3 * f + c] = (float)(s / dA);
+    }
+    return;
+  }
+
+  double m[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  double ga, gb, mu[3] = {0.0, 0.0, 0.0};
+  if (a.mode == MODE_PRECENTERED) {
+    for (int j = 0; j < S; ++j)
+      for (int i = 0; i < 9; ++i) m[i] += base[j * SUMS_STRIDE + i];
+    ga = (double)a.g_target[f];
+    gb = (double)a.g_ref_override;
+  } else {
+    // Exact re-centring of the shifted partial sums (FP64):
+    //   mu = sum_j (sd_j + n_j s_j) / A
+    //   Ga = sum_j (g_j + 2 (s_j - mu) . sd_j + n_j |s_j - mu|^2)
+    //   M  = sum_j (m_j + (s_j - mu) B_j^T),  B_j = sum of reference over split j
+    double sa[3] = {0.0, 0.0, 0.0};
+    for (int j = 0; j < S; ++j) {
+      const double* r = base + j * SUMS_STRIDE;
+      const int32_t q0 = (int32_t)(((int64_t)j * Q) / S), q1 = (int32_t)(((int64_t)(j + 1) * Q) / S);
+      const double nj = (double)(min(4 * q1, A) - 4 * q0);
+      for (int c = 0; c < 3; ++c) sa[c] += r[9 + c] + nj * r[16 + c];
+    }
+    for (int c = 0; c < 3; ++c) mu[c] = sa[c] / dA;
+    ga = 0.0;
+    for (int j = 0; j < S; ++j) {
+      const double* r = base + j * SUMS_STRIDE;
+      const int32_t q0 = (int32_t)(((int64_t)j * Q) / S), q1 = (int32_t)(((int64_t)(j + 1) * Q) / S);
+      const double nj = (double)(min(4 * q1, A) - 4 * q0);
+      double ds[3], bj[3];
+      for (int c = 0; c < 3; ++c) {
+        ds[c] = r[16 + c] - mu[c];
+        bj[c] = a.ref_prefix[3 * (size_t)q1 + c] - a.ref_prefix[3 * (size_t)q0 + c];
+      }
+      ga += r[12] + 2.0 * (ds[0] * r[9] + ds[1] * r[10] + ds[2] * r[11]) +
+            nj * (ds[0] * ds[0] + ds[1] * ds[1] + ds[2] * ds[2]);
+      for (int i = 0; i < 3; ++i)
+        for (int k = 0; k < 3; ++k) m[3 * i + k] += r[3 * i + k] + ds[i] * bj[k];
+    }
+    gb = a.ref_info->g;
+    if (a.out_centroid)
+      for (int c = 0; c < 3; ++c) a.out_centroid[3 * f + c] = (float)mu[c];
+    if (a.out_trace) a.out_trace[f] = (float)ga;
+  }
+
+  bool self = (f == a.self_index);
+  if (self && a.mode == MODE_PRECENTERED) self = (a.g_target[f] == a.g_ref_override);
+  if (self) {
+    a.out_rmsd[f] = 0.f;
+    return;
+  }
+  bool finite = isfinite(ga) && isfinite(gb);
+  for (int i = 0; i < 9; ++i) finite = finite && isfinite(m[i]);
+  if (!finite) {
+    atomicOr(a.err, DEV_ERR_NONFINITE);
+    a.out_rmsd[f] = nanf("");
+    return;
+  }
+  int iters = 0;
+  const double lam = qcp_lambda_max(m, ga, gb, &iters);
+  double msd = (ga + gb - 2.0 * lam) / dA;
+  if (!(msd > 0.0)) msd = 0.0;
+  a.out_rmsd[f] = (float)sqrt(msd);
+
+  // One-pass sums resolve msd to about 1e-7 * scale / sqrt(A); below the
+  // threshold the direct residual is recomputed (see refine_kernel).
+  const double scale = (ga + gb) / (2.0 * dA);
+  const double thr = 0.1 * scale / sqrt(dA);
+  if (msd < thr * thr && A > 0) {
+    double rot[9];
+    qcp_rotation(m, lam, rot);
+    const int slot = atomicAdd(a.refine_count, 1);
+    RefineEntry e;
+    e.frame = f;
+    for (int i = 0; i < 9; ++i) e.rot[i] = (float)rot[i];
+    for (int c = 0; c < 3; ++c) {
+      e.mu_hi[c] = (float)mu[c];
+      e.mu_lo[c] = (float)(mu[c] - (double)e.mu_hi[c]);
+    }
+    e.pad = 0.f;
+    a.refine[slot] = e;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Refinement: direct residual for near-identical frames (warp per frame)
+// ---------------------------------------------------------------------------
+
+struct RefineArgs {
+  const float* x;
+  int32_t n_atoms;
+  int32_t n_padded;
+  int64_t frame_stride;
+  const float* ref;
+  const RefineEntry* list;
+  const int* count;
+  float* out_rmsd;
+};
+
+template <int LAYOUT>
+__global__ void __launch_bounds__(256) refine_kernel(const RefineArgs r) {
+  const int lane = threadIdx.x & 31;
+  const int64_t W = (int64_t)gridDim.x * (blockDim.x >> 5);
+  const int64_t gw = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int n = *reinterpret_cast<const volatile int*>(r.count);
+  const int32_t A = r.n_atoms, Ap = r.n_padded, Q = (A + 3) >> 2;
+  for (int64_t e = gw; e < n; e += W) {
+    const RefineEntry en = r.list[e];
+    const float* fr = r.x + en.frame * r.frame_stride;
+    CF acc = cf_zero();
+    for (int32_t q = lane; q < Q; q += 32) {
+      float ax[4], ay[4], az[4], bx[4], by[4], bz[4];
+      if (LAYOUT == ATOM_MAJOR) {
+        const float4 t0 = ldg4(fr + 12 * (size_t)q), t1 = ldg4(fr + 12 * (size_t)q + 4),
+                     t2 = ldg4(fr + 12 * (size_t)q + 8);
+        ax[0] = t0.x; ay[0] = t0.y; az[0] = t0.z; ax[1] = t0.w;
+        ay[1] = t1.x; az[1] = t1.y; ax[2] = t1.z; ay[2] = t1.w;
+        az[2] = t2.x; ax[3] = t2.y; ay[3] = t2.z; az[3] = t2.w;
+      } else {
+        const float4 tx = ldg4(fr + 4 * (size_t)q), ty = ldg4(fr + Ap + 4 * (size_t)q),
+                     tz = ldg4(fr + 2 * (size_t)Ap + 4 * (size_t)q);
+        ax[0] = tx.x; ax[1] = tx.y; ax[2] = tx.z; ax[3] = tx.w;
+        ay[0] = ty.x; ay[1] = ty.y; ay[2] = ty.z; ay[3] = ty.w;
+        az[0] = tz.x; az[1] = tz.y; az[2] = tz.z; az[3] = tz.w;
+      }
+      load_ref_quad<LAYOUT, false>(r.ref, Ap, q, bx, by, bz);
+      const int nv = A - 4 * q;
+      float part = 0.f;
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        if (t < nv) {
+          const float dx = (ax[t] - en.mu_hi[0]) - en.mu_lo[0];
+          const float dy = (ay[t] - en.mu_hi[1]) - en.mu_lo[1];
+          const float dz = (az[t] - en.mu_hi[2]) - en.mu_lo[2];
+          const float rx = fmaf(en.rot[0], dx, fmaf(en.rot[1], dy, en.rot[2] * dz)) - bx[t];
+          const float ry = fmaf(en.rot[3], dx, fmaf(en.rot[4], dy, en.rot[5] * dz)) - by[t];
+          const float rz = fmaf(en.rot[6], dx, fmaf(en.rot[7], dy, en.rot[8] * dz)) - bz[t];
+          part = fmaf(rx, rx, part);
+          part = fmaf(ry, ry, part);
+          part = fmaf(rz, rz, part);
+        }
+      }
+      cf_add(acc, part);
+    }
+#pragma unroll
+    for (int m = 16; m >= 1; m >>= 1) {
+      CF o;
+      o.hi = __shfl_xor_sync(FULL_MASK, acc.hi, m);
+      o.lo = __shfl_xor_sync(FULL_MASK, acc.lo, m);
+      acc = cf_add2(acc, o);
+    }
+    if (lane == 0) {
+      double msd = cf_to_double(acc) / (double)A;
+      if (!(msd > 0.0)) msd = 0.0;
+      r.out_rmsd[en.frame] = (float)sqrt(msd);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// In-place centring write-back (warp per frame)
+// ---------------------------------------------------------------------------
+
+template <int LAYOUT>
+__global__ void __launch_bounds__(256) center_writeback_kernel(float* x, int64_t F, int32_t A, int32_t Ap,
+                                                               int64_t frame_stride, const float* centroid,
+                                                               float* traces) {
+  const int lane = threadIdx.x & 31;
+  const int64_t W = (int64_t)gridDim.x * (blockDim.x >> 5);
+  const int64_t gw = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int32_t Q = (A + 3) >> 2;
+  for (int64_t f = gw; f < F; f += W) {
+    float* fr = x + f * frame_stride;
+    const float mx = centroid[3 * f], my = centroid[3 * f + 1], mz = centroid[3 * f + 2];
+    CF acc = cf_zero();
+    for (int32_t q = lane; q < Q; q += 32) {
+      const int nv = A - 4 * q;
+      float part = 0.f;
+      if (LAYOUT == ATOM_MAJOR) {
+        float4* p4 = reinterpret_cast<float4*>(fr + 12 * (size_t)q);
+        float v[12];
+        float4 t0 = p4[0], t1 = p4[1], t2 = p4[2];
+        v[0] = t0.x; v[1] = t0.y; v[2] = t0.z; v[3] = t0.w; v[4] = t1.x; v[5] = t1.y;
+        v[6] = t1.z; v[7] = t1.w; v[8] = t2.x; v[9] = t2.y; v[10] = t2.z; v[11] = t2.w;
+        const float mu[3] = {mx, my, mz};
+#pragma unroll
+        for (int e = 0; e < 12; ++e) {
+          if (e / 3 < nv) {
+            v[e] = __fsub_rn(v[e], mu[e % 3]);
+            // float square, then extended-precision accumulation (center_arm.h:78-86)
+            cf_add(acc, __fmul_rn(v[e], v[e]));
+          }
+        }
+        p4[0] = make_float4(v[0], v[1], v[2], v[3]);
+        p4[1] = make_float4(v[4], v[5], v[6], v[7]);
+        p4[2] = make_float4(v[8], v[9], v[10], v[11]);
+      } else {
+        const float mu[3] = {mx, my, mz};
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          float4* p4 = reinterpret_cast<float4*>(fr + (size_t)c * Ap + 4 * (size_t)q);
+          float4 t = *p4;
+          float v[4] = {t.x, t.y, t.z, t.w};
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            if (e < nv) {
+              v[e] = __fsub_rn(v[e], mu[c]);
+              cf_add(acc, __fmul_rn(v[e], v[e]));
+            }
+          }
+          *p4 = make_float4(v[0], v[1], v[2], v[3]);
+        }
+      }
+      (void)part;
+    }
+#pragma unroll
+    for (int m = 16; m >= 1; m >>= 1) {
+      CF o;
+      o.hi = __shfl_xor_sync(FULL_MASK, acc.hi, m);
+      o.lo = __shfl_xor_sync(FULL_MASK, acc.lo, m);
+      acc = cf_add2(acc, o);
+    }
+    if (lane == 0) traces[f] = (float)cf_to_double(acc);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+
+struct StreamCfg {
+  int cq;
+  int nstage;
+  bool ref_smem;
+};
+
+size_t stream_smem_bytes(const StreamCfg& c, int32_t Ap, bool use_ref) {
+  const size_t ref = (c.ref_smem && use_ref) ? align_up((size_t)Ap * 12, 128) : 0;
+  return ref + (size_t)kWarps * c.nstage * c.cq * 48 + (size_t)kWarps * c.nstage * 8;
+}
+
+StreamCfg choose_cfg(int32_t Ap, bool use_ref) {
+  const size_t limit = (size_t)max_dyn_smem();
+  const StreamCfg cands[3] = {{128, 3, true}, {64, 4, true}, {128, 4, false}};
+  for (int i = 0; i < 3; ++i) {
+    if (!use_ref && cands[i].ref_smem) continue;
+    if (stream_smem_bytes(cands[i], Ap, use_ref) <= limit) return cands[i];
+  }
+  return cands[2];
+}
+
+int32_t choose_splits(int64_t F, int32_t Q, int grid_warps) {
+  if (F <= 0) return 1;
+  const int64_t target = 16LL * grid_warps;
+  if (F >= target) return 1;
+  int64_t s = (target + F - 1) / F;
+  int64_t smax = Q / 32;
+  if (smax < 1) smax = 1;
+  if (s > smax) s = smax;
+  if (s < 1) s = 1;
+  return (int32_t)s;
+}
+
+template <int LAYOUT, int MODE, int CQ, int NSTAGE, bool REF_SMEM>
+int launch_stream_t(const StreamArgs& a, size_t smem, int grid, cudaStream_t st) {
+  auto k = stream_kernel<LAYOUT, MODE, CQ, NSTAGE, REF_SMEM>;
+  GB_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+              "cudaFuncSetAttribute(stream_kernel)");
+  k<<<grid, kWarps * 32, smem, st>>>(a);
+  GB_CUDA_TRY(cudaGetLastError(), "launch stream_kernel");
+  return GBRMSD_OK;
+}
+
+template <int LAYOUT, int MODE>
+int launch_stream_m(const StreamArgs& a, const StreamCfg& c, size_t smem, int grid, cudaStream_t st) {
+  if (c.cq == 128 && c.nstage == 3 && c.ref_smem) return launch_stream_t<LAYOUT, MODE, 128, 3, true>(a, smem, grid, st);
+  if (c.cq == 64 && c.nstage == 4 && c.ref_smem) return launch_stream_t<LAYOUT, MODE, 64, 4, true>(a, smem, grid, st);
+  return launch_stream_t<LAYOUT, MODE, 128, 4, false>(a, smem, grid, st);
+}
+
+template <int LAYOUT>
+int launch_stream_l(int mode, const StreamArgs& a, const StreamCfg& c, size_t smem, int grid, cudaStream_t st) {
+  switch (mode) {
+    case MODE_CENTER: return launch_stream_m<LAYOUT, MODE_CENTER>(a, c, smem, grid, st);
+    case MODE_PRECENTERED: return launch_stream_m<LAYOUT, MODE_PRECENTERED>(a, c, smem, grid, st);
+    case MODE_NOSUPERPOSE: return launch_stream_m<LAYOUT, MODE_NOSUPERPOSE>(a, c, smem, grid, st);
+    default: return launch_stream_m<LAYOUT, MODE_TRACE>(a, c, smem, grid, st);
+  }
+}
+
+int launch_stream(int layout, int mode, const StreamArgs& a, cudaStream_t st) {
+  const bool use_ref = mode != MODE_TRACE;
+  const StreamCfg c = choose_cfg(a.n_padded, use_ref);
+  const size_t smem = stream_smem_bytes(c, a.n_padded, use_ref);
+  const int grid = sm_count();
+  return layout == ATOM_MAJOR ? launch_stream_l<ATOM_MAJOR>(mode, a, c, smem, grid, st)
+                              : launch_stream_l<AXIS_MAJOR>(mode, a, c, smem, grid, st);
+}
+
+struct WsLayout {
+  size_t sums_off, refine_off, cent_off, total;
+};
+
+WsLayout ws_layout(int64_t F, int32_t S) {
+  WsLayout w;
+  w.sums_off = HDR_BYTES;
+  w.refine_off = align_up(w.sums_off + (size_t)F * S * SUMS_STRIDE * sizeof(double), 256);
+  w.cent_off = align_up(w.refine_off + (size_t)F * sizeof(RefineEntry), 256);
+  w.total = align_up(w.cent_off + (size_t)F * 3 * sizeof(float), 256);
+  return w;
+}
+
+struct RefWsLayout {
+  size_t info_off, coords_off, prefix_off, total;
+};
+
+RefWsLayout ref_ws_layout(int32_t A, int32_t Ap) {
+  RefWsLayout r;
+  r.info_off = 0;
+  r.coords_off = 256;
+  r.prefix_off = align_up(r.coords_off + (size_t)Ap * 12, 256);
+  const size_t Q = (size_t)((A + 3) / 4);
+  r.total = align_up(r.prefix_off + (Q + 1) * 3 * sizeof(double), 256);
+  return r;
+}
+
+int check_frames(const float* x, int64_t F, int32_t A, int32_t Ap, int64_t frame_stride, int32_t layout) {
+  if (F < 0 || A < 0) return set_error(GBRMSD_E_INVALID, "negative n_frames/n_atoms");
+  if (layout != ATOM_MAJOR && layout != AXIS_MAJOR) return set_error(GBRMSD_E_INVALID, "bad layout %d", layout);
+  if (Ap < A || (Ap & 3)) return set_error(GBRMSD_E_INVALID, "n_padded (%d) must be >= n_atoms (%d) and a multiple of 4", Ap, A);
+  if (frame_stride < 3LL * Ap || (frame_stride & 3))
+    return set_error(GBRMSD_E_INVALID, "frame_stride (%lld) must be >= 3*n_padded and a multiple of 4", (long long)frame_stride);
+  if (F > 0 && A > 0 && (!x || !aligned16(x))) return set_error(GBRMSD_E_INVALID, "coordinates must be a 16-byte aligned device pointer");
+  return GBRMSD_OK;
+}
+
+}  // namespace
+
+int32_t rmsd_splits(int64_t F, int32_t A) {
+  return choose_splits(F, (A + 3) / 4, sm_count() * kWarps);
+}
+
+// Optional CUDA-event timing of the streaming kernel (the dominant kernel):
+// one event pair per gbrmsd_rmsd_to_reference call, recorded on its launch
+// stream, kept in a ring of up to kProfMax calls.
+namespace {
+constexpr int kProfMax = 4096;
+int g_prof_cap = 0;
+int g_prof_n = 0;
+cudaEvent_t g_ev[kProfMax][2];
+}  // namespace
+
+static void prof_begin(cudaStream_t st) {
+  if (g_prof_n < g_prof_cap) cudaEventRecord(g_ev[g_prof_n][0], st);
+}
+
+static void prof_end(cudaStream_t st) {
+  if (g_prof_n < g_prof_cap) {
+    cudaEventRecord(g_ev[g_prof_n][1], st);
+    ++g_prof_n;
+  }
+}
+
+}  // namespace gb
+
+using namespace gb;
+
+extern "C" {
+
+size_t gbrmsd_reference_workspace_bytes(int32_t n_atoms, int32_t n_padded) {
+  if (n_atoms < 0 || n_padded < n_atoms) return 0;
+  return ref_ws_layout(n_atoms, n_padded).total;
+}
+
+int gbrmsd_prepare_reference(const float* ref_xyz, int32_t n_atoms, int32_t n_padded, int32_t layout,
+                             int32_t centre, void* ref_ws, size_t ref_ws_bytes, void* stream) {
+  clear_error();
+  if (n_atoms < 0 || n_padded < n_atoms || (n_padded & 3))
+    return set_error(GBRMSD_E_INVALID, "prepare_reference: n_padded must be >= n_atoms and a multiple of 4");
+  if (layout != ATOM_MAJOR && layout != AXIS_MAJOR) return set_error(GBRMSD_E_INVALID, "prepare_reference: bad layout");
+  const RefWsLayout L = ref_ws_layout(n_atoms, n_padded);
+  if (!ref_ws || ref_ws_bytes < L.total)
+    return set_error(GBRMSD_E_WORKSPACE, "prepare_reference: workspace needs %zu bytes", L.total);
+  if (n_atoms > 0 && !ref_xyz) return set_error(GBRMSD_E_INVALID, "prepare_reference: null reference");
+  unsigned char* w = static_cast<unsigned char*>(ref_ws);
+  ref_prepare_kernel<<<1, PREP_THREADS, 0, static_cast<cudaStream_t>(stream)>>>(
+      ref_xyz, n_atoms, n_padded, layout, centre ? 1 : 0, reinterpret_cast<float*>(w + L.coords_off),
+      reinterpret_cast<RefInfo*>(w + L.info_off), reinterpret_cast<double*>(w + L.prefix_off));
+  GB_CUDA_TRY(cudaGetLastError(), "launch ref_prepare_kernel");
+  return GBRMSD_OK;
+}
+
+int gbrmsd_reference_info(const void* ref_ws, float* host_trace, float* host_centroid3, void* stream) {
+  clear_error();
+  if (!ref_ws) return set_error(GBRMSD_E_INVALID, "reference_info: null workspace");
+  RefInfo ri;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  GB_CUDA_TRY(cudaMemcpyAsync(&ri, ref_ws, sizeof(RefInfo), cudaMemcpyDeviceToHost, st), "copy RefInfo");
+  GB_CUDA_TRY(cudaStreamSynchronize(st), "sync RefInfo");
+  if (host_trace) *host_trace = (float)ri.g;
+  if (host_centroid3)
+    for (int c = 0; c < 3; ++c) host_centroid3[c] = ri.centroid[c];
+  return GBRMSD_OK;
+}
+
+size_t gbrmsd_rmsd_workspace_bytes(int64_t n_frames, int32_t n_atoms) {
+  if (n_frames < 0 || n_atoms < 0) return 0;
+  return ws_layout(n_frames, rmsd_splits(n_frames, n_atoms)).total;
+}
+
+int gbrmsd_rmsd_to_reference(const float* x, int64_t n_frames, int32_t n_atoms, int32_t n_padded,
+                             int64_t frame_stride, int32_t layout, int32_t mode, const void* ref_ws,
+                             const float* g_target, float g_ref, int64_t self_index, float* out_rmsd,
+                             float* out_centroid, float* out_trace, void* ws, size_t ws_bytes,
+                             void* stream) {
+  clear_error();
+  int rc = check_frames(x, n_frames, n_atoms, n_padded, frame_stride, layout);
+  if (rc) return rc;
+  if (mode != MODE_CENTER && mode != MODE_PRECENTERED && mode != MODE_NOSUPERPOSE)
+    return set_error(GBRMSD_E_INVALID, "rmsd_to_reference: bad mode %d", mode);
+  if (n_frames == 0) return GBRMSD_OK;
+  if (!out_rmsd) return set_error(GBRMSD_E_INVALID, "rmsd_to_reference: null out_rmsd");
+  if (!ref_ws) return set_error(GBRMSD_E_INVALID, "rmsd_to_reference: null reference workspace");
+  if (mode == MODE_PRECENTERED && !g_target) return set_error(GBRMSD_E_INVALID, "precentered mode needs g_target");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (n_atoms == 0) {
+    // The reference divides 0/0 and clamps NaN to 0 (theobald_rmsd.cpp:275-277).
+    GB_CUDA_TRY(cudaMemsetAsync(out_rmsd, 0, sizeof(float) * n_frames, st), "memset rmsd");
+    if (out_centroid) GB_CUDA_TRY(cudaMemsetAsync(out_centroid, 0, sizeof(float) * 3 * n_frames, st), "memset");
+    if (out_trace) GB_CUDA_TRY(cudaMemsetAsync(out_trace, 0, sizeof(float) * n_frames, st), "memset");
+    return GBRMSD_OK;
+  }
+  const int32_t S = rmsd_splits(n_frames, n_atoms);
+  const WsLayout L = ws_layout(n_frames, S);
+  if (!ws || ws_bytes < L.total || !aligned16(ws))
+    return set_error(GBRMSD_E_WORKSPACE, "rmsd_to_reference: workspace needs %zu bytes (16-byte aligned)", L.total);
+  const RefWsLayout RL = ref_ws_layout(n_atoms, n_padded);
+  const unsigned char* rw = static_cast<const unsigned char*>(ref_ws);
+  unsigned char* w = static_cast<unsigned char*>(ws);
+  WsHeader* hdr = reinterpret_cast<WsHeader*>(w);
+  GB_CUDA_TRY(cudaMemsetAsync(hdr, 0, sizeof(WsHeader), st), "memset workspace header");
+
+  StreamArgs sa;
+  sa.x = x;
+  sa.n_frames = n_frames;
+  sa.n_atoms = n_atoms;
+  sa.n_padded = n_padded;
+  sa.frame_stride = frame_stride;
+  sa.ref = reinterpret_cast<const float*>(rw + RL.coords_off);
+  sa.splits = S;
+  sa.sums = reinterpret_cast<double*>(w + L.sums_off);
+  sa.err = &hdr->err;
+  prof_begin(st);
+  rc = launch_stream(layout, mode, sa, st);
+  if (rc) return rc;
+  prof_end(st);
+
+  FinishArgs fa;
+  fa.n_frames = n_frames;
+  fa.n_atoms = n_atoms;
+  fa.splits = S;
+  fa.sums = sa.sums;
+  fa.ref_info = reinterpret_cast<const RefInfo*>(rw + RL.info_off);
+  fa.ref_prefix = reinterpret_cast<const double*>(rw + RL.prefix_off);
+  fa.g_target = g_target;
+  fa.g_ref_override = g_ref;
+  fa.self_index = self_index;
+  fa.out_rmsd = out_rmsd;
+  fa.out_centroid = out_centroid;
+  fa.out_trace = out_trace;
+  fa.refine = reinterpret_cast<RefineEntry*>(w + L.refine_off);
+  fa.refine_count = &hdr->refine_count;
+  fa.err = &hdr->err;
+  fa.mode = mode;
+  const int fb = (int)((n_frames + 255) / 256);
+  finish_kernel<<<fb, 256, 0, st>>>(fa);
+  GB_CUDA_TRY(cudaGetLastError(), "launch finish_kernel");
+
+  if (mode != MODE_NOSUPERPOSE) {
+    RefineArgs ra;
+    ra.x = x;
+    ra.n_atoms = n_atoms;
+    ra.n_padded = n_padded;
+    ra.frame_stride = frame_stride;
+    ra.ref = sa.ref;
+    ra.list = fa.refine;
+    ra.count = fa.refine_count;
+    ra.out_rmsd = out_rmsd;
+    if (layout == ATOM_MAJOR)
+      refine_kernel<ATOM_MAJOR><<<sm_count(), 256, 0, st>>>(ra);
+    else
+      refine_kernel<AXIS_MAJOR><<<sm_count(), 256, 0, st>>>(ra);
+    GB_CUDA_TRY(cudaGetLastError(), "launch refine_kernel");
+  }
+  return GBRMSD_OK;
+}
+
+int gbrmsd_center_inplace(float* x, int64_t n_frames, int32_t n_atoms, int32_t n_padded, int64_t frame_stride,
+                          int32_t layout, float* out_traces, float* out_centroids, void* ws, size_t ws_bytes,
+                          void* stream) {
+  clear_error();
+  int rc = check_frames(x, n_frames, n_atoms, n_padded, frame_stride, layout);
+  if (rc) return rc;
+  if (n_frames == 0) return GBRMSD_OK;
+  if (!out_traces) return set_error(GBRMSD_E_INVALID, "center_inplace: null out_traces");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (n_atoms == 0) {
+    GB_CUDA_TRY(cudaMemsetAsync(out_traces, 0, sizeof(float) * n_frames, st), "memset traces");
+    if (out_centroids) GB_CUDA_TRY(cudaMemsetAsync(out_centroids, 0, sizeof(float) * 3 * n_frames, st), "memset");
+    return GBRMSD_OK;
+  }
+  const int32_t S = rmsd_splits(n_frames, n_atoms);
+  const WsLayout L = ws_layout(n_frames, S);
+  const size_t need = L.total;
+  if (!ws || ws_bytes < need || !aligned16(ws))
+    return set_error(GBRMSD_E_WORKSPACE, "center_inplace: workspace needs %zu bytes", need);
+  unsigned char* w = static_cast<unsigned char*>(ws);
+  WsHeader* hdr = reinterpret_cast<WsHeader*>(w);
+  float* cent = out_centroids ? out_centroids : reinterpret_cast<float*>(w + L.cent_off);
+  GB_CUDA_TRY(cudaMemsetAsync(hdr, 0, sizeof(WsHeader), st), "memset workspace header");
+  StreamArgs sa;
+  sa.x = x;
+  sa.n_frames = n_frames;
+  sa.n_atoms = n_atoms;
+  sa.n_padded = n_padded;
+  sa.frame_stride = frame_stride;
+  sa.ref = nullptr;
+  sa.splits = S;
+  sa.sums = reinterpret_cast<double*>(w + L.sums_off);
+  sa.err = &hdr->err;
+  rc = launch_stream(layout, MODE_TRACE, sa, st);
+  if (rc) return rc;
+  FinishArgs fa{};
+  fa.n_frames = n_frames;
+  fa.n_atoms = n_atoms;
+  fa.splits = S;
+  fa.sums = sa.sums;
+  fa.out_centroid = cent;
+  fa.err = &hdr->err;
+  fa.mode = MODE_TRACE;
+  fa.self_index = -1;
+  finish_kernel<<<(int)((n_frames + 255) / 256), 256, 0, st>>>(fa);
+  GB_CUDA_TRY(cudaGetLastError(), "launch finish_kernel(trace)");
+  const int grid = sm_count() * 4;
+  if (layout == ATOM_MAJOR)
+    center_writeback_kernel<ATOM_MAJOR><<<grid, 256, 0, st>>>(x, n_frames, n_atoms, n_padded, frame_stride, cent, out_traces);
+  else
+    center_writeback_kernel<AXIS_MAJOR><<<grid, 256, 0, st>>>(x, n_frames, n_atoms, n_padded, frame_stride, cent, out_traces);
+  GB_CUDA_TRY(cudaGetLastError(), "launch center_writeback_kernel");
+  return GBRMSD_OK;
+}
+
+int gbrmsd_profile_enable(int32_t max_calls) {
+  clear_error();
+  if (max_calls < 0 || max_calls > kProfMax)
+    return set_error(GBRMSD_E_INVALID, "profile_enable: max_calls must be in [0, %d]", kProfMax);
+  for (int i = g_prof_cap; i < max_calls; ++i) {
+    GB_CUDA_TRY(cudaEventCreate(&g_ev[i][0]), "cudaEventCreate");
+    GB_CUDA_TRY(cudaEventCreate(&g_ev[i][1]), "cudaEventCreate");
+  }
+  if (max_calls > g_prof_cap) g_prof_cap = max_calls;
+  if (max_calls == 0) g_prof_cap = 0;
+  g_prof_n = 0;
+  return GBRMSD_OK;
+}
+
+int gbrmsd_profile_read(float* stream_kernel_ms, int32_t capacity) {
+  clear_error();
+  if (!stream_kernel_ms && capacity > 0) return set_error(GBRMSD_E_INVALID, "profile_read: null output");
+  const int n = g_prof_n < capacity ? g_prof_n : capacity;
+  for (int i = 0; i < n; ++i) {
+    GB_CUDA_TRY(cudaEventSynchronize(g_ev[i][1]), "cudaEventSynchronize");
+    GB_CUDA_TRY(cudaEventElapsedTime(&stream_kernel_ms[i], g_ev[i][0], g_ev[i][1]), "cudaEventElapsedTime");
+  }
+  g_prof_n = 0;
+  return n;
+}
+
+int gbrmsd_workspace_status(const void* ws, void* stream) {
+  clear_error();
+  if (!ws) return set_error(GBRMSD_E_INVALID, "workspace_status: null workspace");
+  WsHeader h;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  GB_CUDA_TRY(cudaMemcpyAsync(&h, ws, sizeof(h), cudaMemcpyDeviceToHost, st), "copy header");
+  GB_CUDA_TRY(cudaStreamSynchronize(st), "sync");
+  if (h.err) return set_error(GBRMSD_E_DEVICE, "device error word 0x%x (1 = bounded wait expired, 2 = non-finite input)", h.err);
+  return GBRMSD_OK;
+}
+
+}  // extern "C"

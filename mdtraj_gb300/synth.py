@@ -1,0 +1,126 @@
+"""Seeded synthetic trajectories with the shapes and value distributions of
+the benchmark workloads (there is no dataset: every input is generated).
+
+Single reference (md.rmsd workloads):
+    reference = n_atoms points i.i.d. uniform in a `cube` nm cube;
+    frame i   = R_i (reference + N(0, sigma_i^2)) + t_i,
+    R_i a Haar-random rotation (normalised Gaussian quaternion), t_i uniform
+    in [-translate, translate]^3; frame 0 is the reference itself.
+
+Host generators return numpy float32 atom-major arrays (small sizes, tests);
+device generators fill torch CUDA tensors chunk by chunk (benchmark sizes).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+
+def _rot_from_quat_np(q: np.ndarray) -> np.ndarray:
+    q = q / np.linalg.norm(q, axis=-1, keepdims=True)
+    w, x, y, z = q[..., 0], q[..., 1], q[..., 2], q[..., 3]
+    r = np.stack([
+        1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y),
+        2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x),
+        2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y),
+    ], axis=-1)
+    return r.reshape(q.shape[:-1] + (3, 3))
+
+
+def haar_rotations(n: int, rng: np.random.Generator) -> np.ndarray:
+    """n uniformly random rotation matrices (n, 3, 3), float64."""
+    return _rot_from_quat_np(rng.normal(size=(n, 4)))
+
+
+def single_reference_frames(n_frames: int, n_atoms: int, seed: int = 0, sigma=0.05, cube: float = 4.0,
+                            translate: float = 2.0, exact_fraction: float = 0.0):
+    """(reference (A, 3), frames (F, A, 3)) float32; frames[0] == reference.
+
+    sigma: scalar or per-frame array of noise standard deviations (nm).
+    exact_fraction: fraction of frames (chosen at random, excluding 0) that
+    are exact rotated + translated copies (sigma forced to 0).
+    """
+    rng = np.random.default_rng(seed)
+    ref = rng.uniform(0.0, cube, size=(n_atoms, 3))
+    sig = np.broadcast_to(np.asarray(sigma, dtype=np.float64), (n_frames,)).copy()
+    if exact_fraction > 0 and n_frames > 1:
+        k = max(1, int(round(exact_fraction * n_frames)))
+        sig[rng.choice(np.arange(1, n_frames), size=min(k, n_frames - 1), replace=False)] = 0.0
+    rot = haar_rotations(n_frames, rng)
+    t = rng.uniform(-translate, translate, size=(n_frames, 1, 3))
+    noise = rng.normal(size=(n_frames, n_atoms, 3)) * sig[:, None, None]
+    frames = np.einsum("fkj,fij->fki", ref[None] + noise, rot) + t
+    frames[0] = ref
+    return ref.astype(np.float32), np.ascontiguousarray(frames, dtype=np.float32)
+
+
+def log_uniform(rng: np.random.Generator, lo: float, hi: float, size) -> np.ndarray:
+    return np.exp(rng.uniform(math.log(lo), math.log(hi), size=size))
+
+
+# ---------------------------------------------------------------------------
+# Device generators (torch, CUDA)
+# ---------------------------------------------------------------------------
+
+
+def _torch_rot_from_quat(q):
+    import torch
+
+    q = q / q.norm(dim=-1, keepdim=True)
+    w, x, y, z = q.unbind(-1)
+    r = torch.stack([
+        1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y),
+        2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x),
+        2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y),
+    ], dim=-1)
+    return r.reshape(q.shape[:-1] + (3, 3))
+
+
+def device_single_reference(n_frames: int, n_atoms: int, n_padded: int, layout: int, seed: int, device,
+                            sigma_lo: float = 0.05, sigma_hi: float = 0.05, exact_fraction: float = 0.0,
+                            cube: float = 4.0, translate: float = 2.0, chunk: int = 2048):
+    """Fills a padded device buffer with single-reference frames.
+
+    layout 0: (F, n_padded * 3) atom-major; layout 1: (F, 3, n_padded)
+    axis-major.  sigma is log-uniform in [sigma_lo, sigma_hi] per frame;
+    `exact_fraction` of the frames are exact copies.  Returns
+    (reference float32 (A, 3) on device, frames tensor, per-frame sigma on
+    host).  Padding atoms are zero.
+    """
+    import torch
+
+    g = torch.Generator(device=device)
+    g.manual_seed(int(seed))
+    rng = np.random.default_rng(seed)
+    ref = torch.rand((n_atoms, 3), generator=g, device=device, dtype=torch.float64) * cube
+    if sigma_lo == sigma_hi:
+        sig = np.full(n_frames, sigma_lo)
+    else:
+        sig = log_uniform(rng, sigma_lo, sigma_hi, n_frames)
+    if exact_fraction > 0 and n_frames > 1:
+        k = max(1, int(round(exact_fraction * n_frames)))
+        sig[rng.choice(np.arange(1, n_frames), size=min(k, n_frames - 1), replace=False)] = 0.0
+    if layout == 0:
+        out = torch.zeros((n_frames, n_padded * 3), dtype=torch.float32, device=device)
+    else:
+        out = torch.zeros((n_frames, 3, n_padded), dtype=torch.float32, device=device)
+    sig_t = torch.from_numpy(sig).to(device)
+    for s in range(0, n_frames, chunk):
+        e = min(n_frames, s + chunk)
+        n = e - s
+        q = torch.randn((n, 4), generator=g, device=device, dtype=torch.float64)
+        rot = _torch_rot_from_quat(q)
+        t = (torch.rand((n, 1, 3), generator=g, device=device, dtype=torch.float64) * 2 - 1) * translate
+        noise = torch.randn((n, n_atoms, 3), generator=g, device=device, dtype=torch.float64)
+        noise *= sig_t[s:e, None, None]
+        fr = torch.einsum("fkj,fij->fki", ref[None] + noise, rot) + t
+        if s == 0:
+            fr[0] = ref
+        fr = fr.to(torch.float32)
+        if layout == 0:
+            out[s:e].view(n, n_padded, 3)[:, :n_atoms, :] = fr
+        else:
+            out[s:e, :, :n_atoms] = fr.transpose(1, 2)
+        del fr, noise
+    return ref.to(torch.float32), out, sig

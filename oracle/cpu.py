@@ -1,0 +1,115 @@
+"""ORACLE — test infrastructure only (never used by mdtraj_gb300/).
+
+ctypes access to the two CPU implementations built by oracle/Makefile:
+
+* ``port``      — oracle/qcp_port.c, the C restatement of the reference
+                  algorithm (always buildable: gcc + OpenMP);
+* ``reference`` — mdtraj's own CPU kernels (center.cpp, theobald_rmsd.cpp)
+                  compiled from the reference's sources, with a thin driver
+                  (oracle/ref_driver.cpp) replaying the loops of _rmsd.pyx.
+
+Both mutate their inputs exactly like the reference (in-place centring), so
+callers pass copies.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+PORT_SO = HERE / "_build" / "libqcp_port.so"
+REF_SO = HERE / "_ref" / "libref_rmsd.so"
+
+_vp, _i64, _i32 = C.c_void_p, C.c_int64, C.c_int32
+
+
+def build(ref: bool = True) -> None:
+    """Builds the port (and, when its sources are available, the reference)."""
+    subprocess.run(["make", "-s", "-C", str(HERE), "port"], check=True)
+    if ref:
+        subprocess.run(["make", "-s", "-C", str(HERE), "ref"], check=False,
+                       stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+
+
+def _load(path: Path, prefix: str):
+    lib = C.CDLL(str(path))
+    getattr(lib, f"{prefix}_md_rmsd").argtypes = [_vp, _i64, _i32, _vp, _vp]
+    getattr(lib, f"{prefix}_multiple_axis_major").argtypes = [_vp, _vp, _vp, _vp, _i64, _i64, _i32, _vp]
+    getattr(lib, f"{prefix}_multiple_atom_major").argtypes = [_vp, _vp, _vp, _vp, _i64, _i64, _i32, _vp]
+    for fn in (f"{prefix}_md_rmsd", f"{prefix}_multiple_axis_major", f"{prefix}_multiple_atom_major"):
+        getattr(lib, fn).restype = None
+    return lib
+
+
+class CpuRmsd:
+    """One CPU implementation (``kind`` = "port" or "reference")."""
+
+    def __init__(self, kind: str):
+        self.kind = kind
+        if kind == "port":
+            if not PORT_SO.exists():
+                build(ref=False)
+            self.lib = _load(PORT_SO, "port")
+            self.prefix = "port"
+            self.lib.port_center_and_trace.argtypes = [_vp, _vp, _i64, _i32]
+            self.lib.port_nosuperpose.argtypes = [_vp, _i64, _i32, _vp, _vp]
+        elif kind == "reference":
+            if not REF_SO.exists():
+                build(ref=True)
+            if not REF_SO.exists():
+                raise FileNotFoundError("reference CPU kernels could not be built (no sources)")
+            self.lib = _load(REF_SO, "ref")
+            self.prefix = "ref"
+            self.lib.ref_center_inplace.argtypes = [_vp, _i64, _i32, _vp]
+        else:
+            raise ValueError(kind)
+
+    def md_rmsd(self, target: np.ndarray, ref_frame: np.ndarray) -> np.ndarray:
+        """md.rmsd(target, ref) semantics; centres both arrays in place."""
+        assert target.dtype == np.float32 and target.flags.c_contiguous
+        assert ref_frame.dtype == np.float32 and ref_frame.flags.c_contiguous
+        out = np.empty(target.shape[0], dtype=np.float32)
+        getattr(self.lib, f"{self.prefix}_md_rmsd")(target.ctypes.data, target.shape[0], target.shape[1],
+                                                     ref_frame.ctypes.data, out.ctypes.data)
+        return out
+
+    def multiple(self, xyz1, xyz2, g1, g2, frame: int, axis_major: bool) -> np.ndarray:
+        n_atoms = xyz1.shape[2] if axis_major else xyz1.shape[1]
+        out = np.empty(xyz2.shape[0], dtype=np.float32)
+        fn = getattr(self.lib, f"{self.prefix}_multiple_{'axis' if axis_major else 'atom'}_major")
+        fn(xyz1.ctypes.data, xyz2.ctypes.data, g1.ctypes.data, g2.ctypes.data, frame, xyz2.shape[0], n_atoms,
+           out.ctypes.data)
+        return out
+
+    def center_inplace(self, xyz: np.ndarray) -> np.ndarray:
+        traces = np.empty(xyz.shape[0], dtype=np.float32)
+        if self.kind == "port":
+            self.lib.port_center_and_trace(xyz.ctypes.data, traces.ctypes.data, xyz.shape[0], xyz.shape[1])
+        else:
+            self.lib.ref_center_inplace(xyz.ctypes.data, xyz.shape[0], xyz.shape[1], traces.ctypes.data)
+        return traces
+
+    def nosuperpose(self, target: np.ndarray, ref_frame: np.ndarray) -> np.ndarray:
+        if self.kind != "port":
+            raise NotImplementedError("the reference's msd_nosuperpose lives in Cython")
+        out = np.empty(target.shape[0], dtype=np.float32)
+        self.lib.port_nosuperpose(target.ctypes.data, target.shape[0], target.shape[1], ref_frame.ctypes.data,
+                                  out.ctypes.data)
+        return out
+
+
+def best_available() -> CpuRmsd:
+    """The reference's own kernels when they can be built here, else the port."""
+    try:
+        return CpuRmsd("reference")
+    except (FileNotFoundError, OSError):
+        return CpuRmsd("port")
+
+
+def n_threads() -> int:
+    v = os.environ.get("OMP_NUM_THREADS")
+    return int(v) if v else (os.cpu_count() or 1)

@@ -1,0 +1,215 @@
+"""Generates the golden fixtures in tests/golden/ from the reference itself.
+
+Run in a container that has the reference checkout (default /root/reference,
+override with MDTRAJ_REF); never on the GPU host.  It builds the reference's
+own Cython RMSD extension (mdtraj/rmsd/_rmsd.pyx with its C++ kernels) and
+its XTC reader out of tree under oracle/_ref/py (git-ignored), imports them
+through a stub ``mdtraj`` package, and records:
+
+* frame0_xtc.npz  — examples/data/frame0.xtc (501 frames x 22 atoms) as read
+                    by the reference reader, with the reference's md.rmsd to
+                    frame 0 (plain, precentered, axis-major), its traces and
+                    the FP64 Kabsch values.  The notebook pin
+                    (examples/iterload.ipynb: max 0.18972313 nm at index 44,
+                    from the lossless HDF5 copy) is stored for the test.
+* alignment_6pt.npz — the 6-point known answer of tests/test_alignment.py:29-43
+                    (read from the test file as text): a 90 degree rotation of
+                    the set has RMSD 0.
+* synthetic.npz   — small seeded cases (odd atom counts, exact copies,
+                    degenerate 1-3 atom frames, atom_indices subsets,
+                    superpose=False) with the reference's outputs.
+
+Usage:  python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import ast
+import os
+import shutil
+import subprocess
+import sys
+import types
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parents[2]
+REF = Path(os.environ.get("MDTRAJ_REF", "/root/reference"))
+OUT = Path(__file__).resolve().parent
+BUILD = REPO / "oracle" / "_ref" / "py"
+SRC = REPO / "oracle" / "_ref" / "pysrc"
+
+sys.path.insert(0, str(REPO))
+
+
+def build_reference_python() -> None:
+    """Cythonises the reference's _rmsd and xtc modules from a scratch copy."""
+    if (BUILD / "mdtraj" / "_rmsd.done").exists():
+        return
+    if SRC.exists():
+        shutil.rmtree(SRC)
+    (SRC / "mdtraj" / "formats").mkdir(parents=True)
+    shutil.copytree(REF / "mdtraj" / "rmsd", SRC / "mdtraj" / "rmsd")
+    shutil.copytree(REF / "mdtraj" / "formats" / "xtc", SRC / "mdtraj" / "formats" / "xtc")
+    for p in SRC.rglob("*"):
+        p.chmod(0o755 if p.is_dir() else 0o644)
+    setup = SRC / "setup_ref.py"
+    setup.write_text(
+        f"""
+import numpy as np
+from setuptools import setup, Extension
+from Cython.Build import cythonize
+R = "{SRC}/mdtraj/rmsd"
+X = "{SRC}/mdtraj/formats/xtc"
+simd = ["-msse2", "-mssse3"] if __import__("platform").machine() == "x86_64" else []
+exts = [
+    Extension("mdtraj._rmsd", [f"{{R}}/src/theobald_rmsd.cpp", f"{{R}}/src/rotation.cpp", f"{{R}}/src/center.cpp", f"{{R}}/_rmsd.pyx"],
+              include_dirs=[f"{{R}}/include", np.get_include()], language="c++",
+              extra_compile_args=["-fopenmp", "-O3", "-funroll-loops", "--std=c++11"] + simd, extra_link_args=["-fopenmp"]),
+    Extension("mdtraj.formats.xtc", [f"{{X}}/src/xdrfile.c", f"{{X}}/src/xdr_seek.c", f"{{X}}/src/xdrfile_xtc.c", f"{{X}}/xtc.pyx"],
+              include_dirs=[f"{{X}}/include", X, np.get_include()]),
+]
+setup(name="refbuild", ext_modules=cythonize(exts, language_level=3, force=True),
+      script_args=["build_ext", "--build-lib", "{BUILD}", "--build-temp", "{SRC}/tmp"])
+"""
+    )
+    subprocess.run([sys.executable, str(setup)], check=True, cwd=SRC, stdout=subprocess.DEVNULL)
+    pkg = BUILD / "mdtraj"
+    (pkg / "__init__.py").write_text("")
+    (pkg / "formats" / "__init__.py").write_text("")
+    shutil.copy(REF / "mdtraj" / "formats" / "registry.py", pkg / "formats" / "registry.py")
+    if (pkg / "utils").exists():
+        shutil.rmtree(pkg / "utils")
+    shutil.copytree(REF / "mdtraj" / "utils", pkg / "utils")
+    (pkg / "_rmsd.done").write_text("ok")
+
+
+def import_reference():
+    sys.path.insert(0, str(BUILD))
+    from mdtraj import _rmsd  # noqa: E402
+    from mdtraj.formats import xtc  # noqa: E402
+
+    return _rmsd, xtc
+
+
+class Traj:
+    """Duck-typed stand-in for mdtraj.Trajectory (only .xyz and ._rmsd_traces
+    are read by the reference's rmsd())."""
+
+    def __init__(self, xyz):
+        self.xyz = np.ascontiguousarray(xyz, dtype=np.float32)
+        self._rmsd_traces = None
+
+
+def ref_rmsd(_rmsd, target, ref, frame=0, **kw):
+    t = Traj(np.array(target, copy=True))
+    r = t if ref is target else Traj(np.array(ref, copy=True))
+    return np.asarray(_rmsd.rmsd(t, r, frame, **kw), dtype=np.float32)
+
+
+def frame0_fixture(_rmsd, xtc) -> None:
+    from oracle import fp64
+
+    with xtc.XTCTrajectoryFile(str(REF / "examples" / "data" / "frame0.xtc")) as f:
+        xyz, time, step, box = f.read()
+    xyz = np.ascontiguousarray(xyz, dtype=np.float32)
+    t = Traj(xyz.copy())
+    plain = np.asarray(_rmsd.rmsd(t, t, 0), dtype=np.float32)
+    centred_after = t.xyz.copy()  # md.rmsd centres in place
+    tc = Traj(xyz.copy())
+    traces = np.asarray(_rmsd._center_inplace_atom_major(tc.xyz), dtype=np.float32)
+    tc._rmsd_traces = traces
+    pre = np.asarray(_rmsd.rmsd(tc, tc, 0, precentered=True), dtype=np.float32)
+    axis = np.ascontiguousarray(tc.xyz.transpose(0, 2, 1))
+    axis_rmsd = np.asarray(_rmsd.getMultipleRMSDs_axis_major(axis, axis, traces, traces, 0), dtype=np.float32)
+    pre10 = np.asarray(_rmsd.rmsd(tc, tc, 10, precentered=True), dtype=np.float32)
+    nosup = ref_rmsd(_rmsd, xyz, xyz, 0, superpose=False)
+    sel = np.arange(3, 19)
+    sel_rmsd = ref_rmsd(_rmsd, xyz, xyz, 0, atom_indices=sel)
+    np.savez_compressed(
+        OUT / "frame0_xtc.npz",
+        xyz=xyz,
+        rmsd_frame0=plain,
+        xyz_after_rmsd=centred_after,
+        traces=traces,
+        centred=tc.xyz,
+        rmsd_precentered_frame0=pre,
+        rmsd_precentered_frame10=pre10,
+        rmsd_axis_major_frame0=axis_rmsd,
+        rmsd_nosuperpose_frame0=nosup,
+        atom_indices=sel,
+        rmsd_atom_indices_frame0=sel_rmsd,
+        kabsch_fp64_frame0=fp64.kabsch_rmsd(xyz, xyz[0]),
+        notebook_h5_max=np.float64(0.18972313),
+        notebook_h5_argmax=np.int64(44),
+    )
+    print("frame0: max", plain.max(), "at", int(plain.argmax()), "first", plain[:5])
+
+
+def alignment_fixture() -> None:
+    src = (REF / "tests" / "test_alignment.py").read_text()
+    tree = ast.parse(src)
+    found = {}
+    for node in tree.body:
+        if isinstance(node, ast.Assign) and len(node.targets) == 1 and isinstance(node.targets[0], ast.Name):
+            name = node.targets[0].id
+            if name in ("xyz1", "rotation") and isinstance(node.value, ast.Call):
+                found[name] = np.array(ast.literal_eval(node.value.args[0]), dtype=np.float64)
+    xyz1, rot = found["xyz1"], found["rotation"]
+    offset = np.array([0.25, -1.5, 0.75])
+    xyz2 = rot.dot(xyz1.T).T + offset
+    np.savez_compressed(OUT / "alignment_6pt.npz", xyz1=xyz1.astype(np.float32), xyz2=xyz2.astype(np.float32),
+                        rotation=rot, expected_rmsd=np.float64(0.0), decimal=np.int64(5))
+
+
+def synthetic_fixture(_rmsd) -> None:
+    from mdtraj_gb300 import synth
+    from oracle import fp64
+
+    cases = {}
+    # cfg0-like, odd atom count (not a multiple of 4), frame 0 is the reference
+    ref, x = synth.single_reference_frames(64, 97, seed=11, sigma=0.05)
+    cases["cfg0_small"] = (x, 0)
+    # exact rotated/translated copies (true rmsd 0) and tiny noise
+    ref, x = synth.single_reference_frames(32, 257, seed=12, sigma=np.array([0.0] * 16 + [1e-3] * 16))
+    cases["copies"] = (x, 0)
+    # degenerate structures: 1, 2, 3 atoms; 5 atoms
+    for A in (1, 2, 3, 5):
+        ref, x = synth.single_reference_frames(16, A, seed=20 + A, sigma=0.1)
+        cases[f"atoms{A}"] = (x, 0)
+    # larger frame count, frame != 0
+    ref, x = synth.single_reference_frames(100, 1000, seed=13, sigma=0.05)
+    cases["cfg0_mid"] = (x, 7)
+    arrays = {}
+    for name, (x, frame) in cases.items():
+        arrays[f"{name}__xyz"] = x
+        arrays[f"{name}__frame"] = np.int64(frame)
+        arrays[f"{name}__ref"] = ref_rmsd(_rmsd, x, x, frame)
+        arrays[f"{name}__fp64"] = fp64.kabsch_rmsd(x, x[frame])
+        arrays[f"{name}__nosup"] = ref_rmsd(_rmsd, x, x, frame, superpose=False)
+    # atom_indices / ref_atom_indices with a different reference object
+    ref, x = synth.single_reference_frames(40, 120, seed=14, sigma=0.05)
+    other = np.ascontiguousarray(np.concatenate([x[:5, 60:], x[:5, :60]], axis=1))
+    ai = np.arange(0, 60)
+    rai = np.arange(60, 120)
+    arrays["indices__xyz"] = x
+    arrays["indices__other"] = other
+    arrays["indices__ai"] = ai
+    arrays["indices__rai"] = rai
+    arrays["indices__ref"] = np.asarray(
+        _rmsd.rmsd(Traj(x.copy()), Traj(other.copy()), 2, atom_indices=ai, ref_atom_indices=rai), dtype=np.float32)
+    np.savez_compressed(OUT / "synthetic.npz", **arrays)
+
+
+def main() -> None:
+    build_reference_python()
+    _rmsd, xtc = import_reference()
+    frame0_fixture(_rmsd, xtc)
+    alignment_fixture()
+    synthetic_fixture(_rmsd)
+    for p in sorted(OUT.glob("*.npz")):
+        print(p.name, p.stat().st_size, "bytes")
+
+
+if __name__ == "__main__":
+    main()

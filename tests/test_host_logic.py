@@ -1,0 +1,127 @@
+"""Boundary behaviour of the drop-in that needs no GPU: argument validation
+and errors identical to mdtraj/rmsd/_rmsd.pyx:152-184 and the memmap tests
+(tests/test_rmsd_memmap.py), ensure_type and Trajectory semantics (CPU)."""
+import warnings
+
+import numpy as np
+import pytest
+
+import mdtraj_gb300 as md
+from mdtraj_gb300 import _rmsd
+from mdtraj_gb300.utils import TypeCastPerformanceWarning, ensure_type
+
+
+def traj(F=4, A=6, seed=0):
+    return md.Trajectory(np.random.default_rng(seed).normal(size=(F, A, 3)).astype(np.float32))
+
+
+def test_invalid_atom_indices_raise_value_error():
+    t = traj()
+    with pytest.raises(ValueError, match="atom_indices must be valid"):
+        md.rmsd(t, t, 0, atom_indices=[0, 6])
+    with pytest.raises(ValueError, match="atom_indices must be valid"):
+        md.rmsd(t, t, 0, atom_indices=[-1, 2])
+    with pytest.raises(ValueError, match="ref_atom_indices must be valid"):
+        md.rmsd(t, t, 0, atom_indices=[0, 1], ref_atom_indices=[0, 9])
+    with pytest.raises(ValueError, match="same number of atom indices"):
+        md.rmsd(t, t, 0, atom_indices=[0, 1], ref_atom_indices=[0, 1, 2])
+
+
+def test_frame_out_of_range_and_atom_mismatch():
+    t = traj()
+    with pytest.raises(ValueError, match="Cannot calculate RMSD of frame 4"):
+        md.rmsd(t, t, 4)
+    # different atom counts without indices: the reference evaluates
+    # len(slice) and raises TypeError
+    with pytest.raises(TypeError):
+        md.rmsd(traj(A=6), traj(A=7), 0)
+
+
+def test_wrong_ndim_is_an_assertion():
+    class Obj:
+        xyz = np.zeros((3, 4, 2), dtype=np.float32)
+        _rmsd_traces = None
+
+    with pytest.raises(AssertionError):
+        md.rmsd(Obj(), Obj(), 0)
+
+
+def test_read_only_target_raises_value_error():
+    # tests/test_rmsd_memmap.py:11-56: read-only coordinates cannot be centred
+    t = traj()
+    t._xyz.setflags(write=False)
+    with pytest.raises(ValueError):
+        md.rmsd(t, t, 0)
+    t2 = traj()
+    t2._rmsd_traces = np.ones(4, dtype=np.float32)
+    t2._xyz.setflags(write=False)
+    with pytest.raises(ValueError):
+        md.rmsd(t2, t2, 0, precentered=True)
+
+
+def test_axis_major_argument_checks():
+    x = np.zeros((3, 3, 5), dtype=np.float32)
+    g = np.zeros(3, dtype=np.float32)
+    with pytest.raises(ValueError, match="same number of atoms"):
+        _rmsd.getMultipleRMSDs_axis_major(x, np.zeros((3, 3, 6), dtype=np.float32), g, g, 0)
+    with pytest.raises(ValueError, match="Cannot calculate RMSD of frame 3"):
+        _rmsd.getMultipleRMSDs_axis_major(x, x, g, g, 3)
+    with pytest.raises(AssertionError):
+        _rmsd.getMultipleRMSDs_axis_major(np.zeros((3, 4, 5), np.float32), np.zeros((3, 4, 5), np.float32), g, g, 0)
+    with pytest.raises(ValueError, match="dtype mismatch"):
+        _rmsd.getMultipleRMSDs_axis_major(x.astype(np.float64), x, g, g, 0)
+    with pytest.raises(ValueError, match="C-contiguous"):
+        _rmsd.getMultipleRMSDs_axis_major(np.zeros((3, 5, 3), np.float32).transpose(0, 2, 1), x, g, g, 0)
+    with pytest.raises(TypeError):
+        _rmsd.getMultipleRMSDs_atom_major(None, x, g, g, 0)
+
+
+def test_no_device_means_loud_failure_not_cpu_fallback():
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a CUDA device is present")
+    t = traj()
+    with pytest.raises(RuntimeError, match="no CPU fallback"):
+        md.rmsd(t, t, 0)
+
+
+def test_precentered_warning_paths_emit_runtime_warning():
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("covered by the GPU tests")
+    t = traj()
+    with warnings.catch_warnings(record=True) as w:
+        warnings.simplefilter("always")
+        with pytest.raises(RuntimeError):
+            md.rmsd(t, t, 0, precentered=True)  # no traces: warns, then needs the device
+    assert any("precentered is ignored" in str(x.message) for x in w)
+
+
+def test_ensure_type_semantics():
+    with pytest.warns(TypeCastPerformanceWarning):
+        a = ensure_type(np.arange(3, dtype=np.int32), dtype=np.int64, ndim=1, name="a")
+    assert a.dtype == np.int64
+    with pytest.raises(ValueError, match="must be ndim 2"):
+        ensure_type(np.zeros(3), np.float32, 2, "b")
+    v = ensure_type(np.zeros((4, 3)), np.float32, 3, "xyz", add_newaxis_on_deficient_ndim=True, warn_on_cast=False)
+    assert v.shape == (1, 4, 3) and v.flags.c_contiguous
+    with pytest.raises(ValueError, match="must be shape"):
+        ensure_type(np.zeros((2, 4, 2)), np.float32, 3, "xyz", shape=(None, None, 3), warn_on_cast=False)
+    with pytest.raises(TypeError):
+        ensure_type(3.0, np.float32, 2, "c")
+    assert ensure_type(None, np.float32, 1, "d", can_be_none=True) is None
+
+
+def test_trajectory_contract():
+    t = traj(F=5)
+    assert t.xyz.dtype == np.float32 and t.xyz.flags.c_contiguous
+    t._rmsd_traces = np.arange(5, dtype=np.float32)
+    s = t[1:3]
+    np.testing.assert_array_equal(s._rmsd_traces, [1, 2])
+    np.testing.assert_array_equal(s.xyz, t.xyz[1:3])
+    t.xyz = t.xyz * 2  # setting coordinates invalidates cached traces
+    assert t._rmsd_traces is None
+    one = md.Trajectory(np.zeros((4, 3)))
+    assert one.n_frames == 1 and one.n_atoms == 4
