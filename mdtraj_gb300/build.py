@@ -9,6 +9,7 @@ from __future__ import annotations
 
 import concurrent.futures as cf
 import os
+import platform
 import shutil
 import subprocess
 import sys
@@ -16,8 +17,9 @@ from pathlib import Path
 
 PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
-BUILD = PKG / "_build"
+BUILD = PKG / "_build" / platform.machine()
 LIB = PKG / "libgbrmsd.so"
+STAMP = PKG / "_build" / "libgbrmsd.arch"   # machine the current .so was linked for
 INCLUDE = PKG.parent / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -73,7 +75,7 @@ def _compile(src: Path, verbose: bool) -> Path:
 
 def build(verbose: bool = False, force: bool = False) -> Path:
     """Compiles csrc/*.cu and links libgbrmsd.so; returns the library path."""
-    BUILD.mkdir(exist_ok=True)
+    BUILD.mkdir(parents=True, exist_ok=True)
     sources = sorted(CSRC.glob("*.cu"))
     if force:
         for o in BUILD.glob("*.o"):
@@ -81,7 +83,8 @@ def build(verbose: bool = False, force: bool = False) -> Path:
     jobs = min(len(sources), os.cpu_count() or 4)
     with cf.ThreadPoolExecutor(max_workers=jobs) as ex:
         objs = list(ex.map(lambda s: _compile(s, verbose), sources))
-    if _stale(LIB, objs):
+    arch_ok = STAMP.exists() and STAMP.read_text().strip() == platform.machine()
+    if not arch_ok or _stale(LIB, objs):
         tmp = LIB.with_suffix(".so.tmp")
         cmd = [nvcc(), *ARCH, "-shared", "-cudart", "static", "-o", str(tmp), *map(str, objs)]
         if verbose:
@@ -90,6 +93,7 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
         os.replace(tmp, LIB)
+        STAMP.write_text(platform.machine())
     return LIB
 
 

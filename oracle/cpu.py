@@ -15,14 +15,15 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import platform
 import subprocess
 from pathlib import Path
 
 import numpy as np
 
 HERE = Path(__file__).resolve().parent
-PORT_SO = HERE / "_build" / "libqcp_port.so"
-REF_SO = HERE / "_ref" / "libref_rmsd.so"
+PORT_SO = HERE / "_build" / platform.machine() / "libqcp_port.so"
+REF_SO = HERE / "_ref" / platform.machine() / "libref_rmsd.so"
 
 _vp, _i64, _i32 = C.c_void_p, C.c_int64, C.c_int32
 
