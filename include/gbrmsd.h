@@ -112,6 +112,16 @@ int gbrmsd_center_inplace(float* x, int64_t n_frames, int32_t n_atoms, int32_t n
  * GBRMSD_OK otherwise.  The error word is cleared by the next call. */
 int gbrmsd_workspace_status(const void* ws, void* stream);
 
+/* Launch configurations of the streaming kernel (warps per CTA, quads per
+ * stage, stages per warp, reference in shared memory).  By default the first
+ * configuration whose shared memory fits is used; select(i) forces
+ * configuration i for later calls where it fits (-1 restores the default);
+ * used by the tuner.  describe() writes the 4 parameters and returns 1 if the
+ * configuration fits frames of n_atoms atoms, 0 if not. */
+int gbrmsd_stream_config_count(void);
+int gbrmsd_stream_config_select(int32_t index);
+int gbrmsd_stream_config_describe(int32_t index, int32_t n_atoms, int32_t* out4);
+
 /* Timing of the streaming kernel (the dominant kernel of
  * gbrmsd_rmsd_to_reference) with CUDA events recorded on the caller's stream,
  * for benchmarks.  gbrmsd_profile_enable(n) arms recording for the next n

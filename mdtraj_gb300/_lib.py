@@ -47,6 +47,9 @@ SIGNATURES: dict[str, tuple] = {
     ),
     "gbrmsd_center_inplace": (C.c_int, [_vp, _i64, _i32, _i32, _i64, _i32, _vp, _vp, _vp, _sz, _vp]),
     "gbrmsd_workspace_status": (C.c_int, [_vp, _vp]),
+    "gbrmsd_stream_config_count": (C.c_int, []),
+    "gbrmsd_stream_config_select": (C.c_int, [_i32]),
+    "gbrmsd_stream_config_describe": (C.c_int, [_i32, _i32, _vp]),
     "gbrmsd_profile_enable": (C.c_int, [_i32]),
     "gbrmsd_profile_read": (C.c_int, [_vp, _i32]),
     "gbrmsd_copy_rows": (C.c_int, [_vp, _sz, _vp, _sz, _sz, _sz, _i32, _vp]),

@@ -165,11 +165,17 @@ struct Cursor {
 template <int CQ>
 __device__ __forceinline__ void cursor_unit(Cursor& cur, int64_t u, int32_t S, int32_t Q) {
   cur.unit = u;
+  cur.c = 0;
+  if (S == 1) {
+    cur.frame = u;
+    cur.q0 = 0;
+    cur.q1 = Q;
+    return;
+  }
   cur.frame = u / S;
   const int32_t s = (int32_t)(u - cur.frame * S);
   cur.q0 = (int32_t)(((int64_t)s * Q) / S);
   cur.q1 = (int32_t)(((int64_t)(s + 1) * Q) / S);
-  cur.c = 0;
 }
 
 // Advances to the next chunk; returns true when a new unit starts.
@@ -245,25 +251,79 @@ struct NSums {
   static constexpr int value = MODE == MODE_CENTER ? 13 : MODE == MODE_PRECENTERED ? 9 : MODE == MODE_NOSUPERPOSE ? 1 : 3;
 };
 
-template <int LAYOUT, int MODE, int CQ, int NSTAGE, bool REF_SMEM>
-__global__ void __launch_bounds__(kWarps * 32, 1) stream_kernel(const StreamArgs p) {
+// Level-1 accumulation of one quad (4 atoms).  MASKED handles the last quad
+// of a frame whose atom count is not a multiple of 4 (nv valid atoms).
+template <int MODE, bool MASKED, int NV>
+__device__ __forceinline__ void accum_quad(float (&acc)[NV], const float (&ax)[4], const float (&ay)[4],
+                                           const float (&az)[4], const float (&bx)[4], const float (&by)[4],
+                                           const float (&bz)[4], const float (&shift)[3], int nv) {
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    float dx, dy, dz;
+    if constexpr (MODE == MODE_CENTER) {
+      dx = ax[t] - shift[0]; dy = ay[t] - shift[1]; dz = az[t] - shift[2];
+    } else if constexpr (MODE == MODE_NOSUPERPOSE) {
+      dx = ax[t] - bx[t]; dy = ay[t] - by[t]; dz = az[t] - bz[t];
+    } else {
+      dx = ax[t]; dy = ay[t]; dz = az[t];
+    }
+    if constexpr (MASKED) {
+      if (t >= nv) { dx = 0.f; dy = 0.f; dz = 0.f; }
+    }
+    if constexpr (MODE == MODE_NOSUPERPOSE) {
+      acc[0] = fmaf(dx, dx, acc[0]);
+      acc[0] = fmaf(dy, dy, acc[0]);
+      acc[0] = fmaf(dz, dz, acc[0]);
+    } else {
+      acc[0] = fmaf(dx, bx[t], acc[0]);
+      acc[1] = fmaf(dx, by[t], acc[1]);
+      acc[2] = fmaf(dx, bz[t], acc[2]);
+      acc[3] = fmaf(dy, bx[t], acc[3]);
+      acc[4] = fmaf(dy, by[t], acc[4]);
+      acc[5] = fmaf(dy, bz[t], acc[5]);
+      acc[6] = fmaf(dz, bx[t], acc[6]);
+      acc[7] = fmaf(dz, by[t], acc[7]);
+      acc[8] = fmaf(dz, bz[t], acc[8]);
+      if constexpr (MODE == MODE_CENTER) {
+        acc[9] += dx;
+        acc[10] += dy;
+        acc[11] += dz;
+        float gg = acc[12];
+        gg = fmaf(dx, dx, gg);
+        gg = fmaf(dy, dy, gg);
+        gg = fmaf(dz, dz, gg);
+        acc[12] = gg;
+      }
+    }
+  }
+}
+
+// Streaming pass.  WARPS warps per CTA, each with a private ring of NSTAGE
+// shared-memory stages of CQ quads, fed by bulk async copies that lane 0
+// issues NSTAGE chunks ahead.  FP32 level-1 sums cover at most 4 quads per
+// lane (16 atoms) before they are folded into TwoSum pairs, which bounds the
+// rounding error of the one-pass sums independently of the atom count.
+template <int LAYOUT, int MODE, int CQ, int NSTAGE, bool REF_SMEM, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32, 1) stream_kernel(const StreamArgs p) {
   extern __shared__ __align__(128) unsigned char smem[];
   constexpr int STAGE_BYTES = CQ * 48;
   constexpr int NV = NSums<MODE>::value;
   constexpr bool USE_REF = MODE != MODE_TRACE;
+  constexpr int QPL = CQ / 32;  // quads per lane per full chunk
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
   const int32_t A = p.n_atoms;
   const int32_t Ap = p.n_padded;
   const int32_t Q = (A + 3) >> 2;
   const int32_t S = p.splits;
-  const size_t ref_al = REF_SMEM ? align_up((size_t)Ap * 12, 128) : 0;
+  const bool ragged_tail = (A & 3) != 0;
+  const size_t ref_al = (REF_SMEM && USE_REF) ? align_up((size_t)Ap * 12, 128) : 0;
   float* sref = reinterpret_cast<float*>(smem);
   unsigned char* stages = smem + ref_al + (size_t)warp * NSTAGE * STAGE_BYTES;
   uint64_t* bars =
-      reinterpret_cast<uint64_t*>(smem + ref_al + (size_t)kWarps * NSTAGE * STAGE_BYTES) + warp * NSTAGE;
+      reinterpret_cast<uint64_t*>(smem + ref_al + (size_t)WARPS * NSTAGE * STAGE_BYTES) + warp * NSTAGE;
 
-  if (REF_SMEM && USE_REF) {
+  if constexpr (REF_SMEM && USE_REF) {
     const float4* src = reinterpret_cast<const float4*>(p.ref);
     float4* dst = reinterpret_cast<float4*>(sref);
     const int n4 = Ap * 3 / 4;
@@ -277,10 +337,9 @@ __global__ void __launch_bounds__(kWarps * 32, 1) stream_kernel(const StreamArgs
   const float* rbase = REF_SMEM ? sref : p.ref;
 
   const int64_t n_units = p.n_frames * S;
-  const int64_t W = (int64_t)gridDim.x * kWarps;
-  const int64_t gw = (int64_t)blockIdx.x * kWarps + warp;
+  const int64_t W = (int64_t)gridDim.x * WARPS;
+  const int64_t gw = (int64_t)blockIdx.x * WARPS + warp;
 
-  // Producer cursor runs NSTAGE chunks ahead of the consumer cursor.
   Cursor pc, cc;
   cursor_unit<CQ>(pc, gw, S, Q);
   cursor_unit<CQ>(cc, gw, S, Q);
@@ -299,6 +358,8 @@ __global__ void __launch_bounds__(kWarps * 32, 1) stream_kernel(const StreamArgs
   int slot = 0;
   bool failed = false;
   CF acc2[NV];
+  float acc1[NV];
+  int pending = 0;  // quads per lane in acc1 since the last fold
   float shift[3] = {0.f, 0.f, 0.f};
 
 #pragma unroll 1
@@ -306,7 +367,8 @@ __global__ void __launch_bounds__(kWarps * 32, 1) stream_kernel(const StreamArgs
     const bool unit_start = (cc.c == 0);
     if (unit_start) {
 #pragma unroll
-      for (int j = 0; j < NV; ++j) acc2[j] = cf_zero();
+      for (int j = 0; j < NV; ++j) { acc2[j] = cf_zero(); acc1[j] = 0.f; }
+      pending = 0;
     }
     const int32_t qb = cc.q0 + cc.c * CQ;
     const int32_t nq = min(CQ, cc.q1 - qb);
@@ -319,7 +381,7 @@ __global__ void __launch_bounds__(kWarps * 32, 1) stream_kernel(const StreamArgs
     const float* st = reinterpret_cast<const float*>(stages + slot * STAGE_BYTES);
 
     if (MODE == MODE_CENTER && unit_start) {
-      // Shift = mean of the first atoms of the unit (lane's first quad).
+      // Shift = mean of the unit's first atoms (each lane's first quad).
       float sx = 0.f, sy = 0.f, sz = 0.f, cnt = 0.f;
       if (lane < nq) {
         float x[4], y[4], z[4];
@@ -333,71 +395,49 @@ __global__ void __launch_bounds__(kWarps * 32, 1) stream_kernel(const StreamArgs
       shift[0] = sx / cnt; shift[1] = sy / cnt; shift[2] = sz / cnt;
     }
 
-    float acc1[NV];
+    // The frame's padded last quad can only be the chunk's last quad.
+    const bool has_tail = ragged_tail && (qb + nq == Q);
+    if (nq == CQ && !has_tail) {
 #pragma unroll
-    for (int j = 0; j < NV; ++j) acc1[j] = 0.f;
-
-#pragma unroll
-    for (int kq = 0; kq < CQ / 32; ++kq) {
-      const int i = lane + 32 * kq;
-      if (i < nq) {
+      for (int kq = 0; kq < QPL; ++kq) {
+        const int i = lane + 32 * kq;
         const int32_t gq = qb + i;
-        const int nv = A - 4 * gq;  // >= 1 by construction
         float ax[4], ay[4], az[4];
         load_stage_quad<LAYOUT, CQ>(st, i, ax, ay, az);
-        float bx[4] = {0.f, 0.f, 0.f, 0.f}, by[4] = {0.f, 0.f, 0.f, 0.f}, bz[4] = {0.f, 0.f, 0.f, 0.f};
-        if constexpr (USE_REF) load_ref_quad<LAYOUT, REF_SMEM>(rbase, Ap, gq, bx, by, bz);
         if constexpr (MODE == MODE_TRACE) {
-          // exact centroid: compensated per-atom sums of the raw coordinates
 #pragma unroll
-          for (int t = 0; t < 4; ++t)
-            if (t < nv) { cf_add(acc2[0], ax[t]); cf_add(acc2[1], ay[t]); cf_add(acc2[2], az[t]); }
-          continue;
+          for (int t = 0; t < 4; ++t) { cf_add(acc2[0], ax[t]); cf_add(acc2[1], ay[t]); cf_add(acc2[2], az[t]); }
+        } else {
+          float bx[4], by[4], bz[4];
+          load_ref_quad<LAYOUT, REF_SMEM>(rbase, Ap, gq, bx, by, bz);
+          accum_quad<MODE, false, NV>(acc1, ax, ay, az, bx, by, bz, shift, 4);
         }
+      }
+    } else {
 #pragma unroll
-        for (int t = 0; t < 4; ++t) {
-          const bool ok = t < nv;
-          float dx, dy, dz;
-          if constexpr (MODE == MODE_CENTER) {
-            dx = ax[t] - shift[0]; dy = ay[t] - shift[1]; dz = az[t] - shift[2];
-          } else if constexpr (MODE == MODE_NOSUPERPOSE) {
-            dx = ax[t] - bx[t]; dy = ay[t] - by[t]; dz = az[t] - bz[t];
+      for (int kq = 0; kq < QPL; ++kq) {
+        const int i = lane + 32 * kq;
+        if (i < nq) {
+          const int32_t gq = qb + i;
+          const int nv = A - 4 * gq;
+          float ax[4], ay[4], az[4];
+          load_stage_quad<LAYOUT, CQ>(st, i, ax, ay, az);
+          if constexpr (MODE == MODE_TRACE) {
+#pragma unroll
+            for (int t = 0; t < 4; ++t)
+              if (t < nv) { cf_add(acc2[0], ax[t]); cf_add(acc2[1], ay[t]); cf_add(acc2[2], az[t]); }
           } else {
-            dx = ax[t]; dy = ay[t]; dz = az[t];
-          }
-          if (!ok) { dx = 0.f; dy = 0.f; dz = 0.f; }
-          if constexpr (MODE == MODE_NOSUPERPOSE) {
-            acc1[0] = fmaf(dx, dx, acc1[0]);
-            acc1[0] = fmaf(dy, dy, acc1[0]);
-            acc1[0] = fmaf(dz, dz, acc1[0]);
-          } else {
-            acc1[0] = fmaf(dx, bx[t], acc1[0]);
-            acc1[1] = fmaf(dx, by[t], acc1[1]);
-            acc1[2] = fmaf(dx, bz[t], acc1[2]);
-            acc1[3] = fmaf(dy, bx[t], acc1[3]);
-            acc1[4] = fmaf(dy, by[t], acc1[4]);
-            acc1[5] = fmaf(dy, bz[t], acc1[5]);
-            acc1[6] = fmaf(dz, bx[t], acc1[6]);
-            acc1[7] = fmaf(dz, by[t], acc1[7]);
-            acc1[8] = fmaf(dz, bz[t], acc1[8]);
-            if constexpr (MODE == MODE_CENTER) {
-              acc1[9] += dx;
-              acc1[10] += dy;
-              acc1[11] += dz;
-              float gg = acc1[12];
-              gg = fmaf(dx, dx, gg);
-              gg = fmaf(dy, dy, gg);
-              gg = fmaf(dz, dz, gg);
-              acc1[12] = gg;
-            }
+            float bx[4], by[4], bz[4];
+            load_ref_quad<LAYOUT, REF_SMEM>(rbase, Ap, gq, bx, by, bz);
+            if (nv < 4)
+              accum_quad<MODE, true, NV>(acc1, ax, ay, az, bx, by, bz, shift, nv);
+            else
+              accum_quad<MODE, false, NV>(acc1, ax, ay, az, bx, by, bz, shift, 4);
           }
         }
       }
     }
-    if constexpr (MODE != MODE_TRACE) {
-#pragma unroll
-      for (int j = 0; j < NV; ++j) cf_add(acc2[j], acc1[j]);
-    }
+    pending += QPL;
 
     // Release the stage and refill it with the chunk NSTAGE ahead.
     __syncwarp();
@@ -413,6 +453,13 @@ __global__ void __launch_bounds__(kWarps * 32, 1) stream_kernel(const StreamArgs
 
     const int64_t unit = cc.unit;
     const bool unit_end = cursor_next<CQ>(cc, W, S, Q);
+    if constexpr (MODE != MODE_TRACE) {
+      if (pending >= 4 || unit_end) {
+#pragma unroll
+        for (int j = 0; j < NV; ++j) { cf_add(acc2[j], acc1[j]); acc1[j] = 0.f; }
+        pending = 0;
+      }
+    }
     if (unit_end) {
       double* rec = p.sums + unit * SUMS_STRIDE;
       if constexpr (NV == 1) {
@@ -591,7 +638,48 @@ struct RefineArgs {
 };
 
 template <int LAYOUT>
+__device__ __forceinline__ void load_frame_quad(const float* fr, int32_t Ap, int32_t q, float (&x)[4], float (&y)[4],
+                                                float (&z)[4]) {
+  if (LAYOUT == ATOM_MAJOR) {
+    const float4 t0 = ldg4(fr + 12 * (size_t)q), t1 = ldg4(fr + 12 * (size_t)q + 4),
+                 t2 = ldg4(fr + 12 * (size_t)q + 8);
+    x[0] = t0.x; y[0] = t0.y; z[0] = t0.z; x[1] = t0.w;
+    y[1] = t1.x; z[1] = t1.y; x[2] = t1.z; y[2] = t1.w;
+    z[2] = t2.x; x[3] = t2.y; y[3] = t2.z; z[3] = t2.w;
+  } else {
+    const float4 tx = ldg4(fr + 4 * (size_t)q), ty = ldg4(fr + Ap + 4 * (size_t)q),
+                 tz = ldg4(fr + 2 * (size_t)Ap + 4 * (size_t)q);
+    x[0] = tx.x; x[1] = tx.y; x[2] = tx.z; x[3] = tx.w;
+    y[0] = ty.x; y[1] = ty.y; y[2] = ty.z; y[3] = ty.w;
+    z[0] = tz.x; z[1] = tz.y; z[2] = tz.z; z[3] = tz.w;
+  }
+}
+
+// sum over valid atoms of |R (a - mu) - b|^2 for one quad
+__device__ __forceinline__ float residual_quad(const RefineEntry& en, const float (&ax)[4], const float (&ay)[4],
+                                               const float (&az)[4], const float (&bx)[4], const float (&by)[4],
+                                               const float (&bz)[4], int nv) {
+  float part = 0.f;
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    if (t < nv) {
+      const float dx = (ax[t] - en.mu_hi[0]) - en.mu_lo[0];
+      const float dy = (ay[t] - en.mu_hi[1]) - en.mu_lo[1];
+      const float dz = (az[t] - en.mu_hi[2]) - en.mu_lo[2];
+      const float rx = fmaf(en.rot[0], dx, fmaf(en.rot[1], dy, en.rot[2] * dz)) - bx[t];
+      const float ry = fmaf(en.rot[3], dx, fmaf(en.rot[4], dy, en.rot[5] * dz)) - by[t];
+      const float rz = fmaf(en.rot[6], dx, fmaf(en.rot[7], dy, en.rot[8] * dz)) - bz[t];
+      part = fmaf(rx, rx, part);
+      part = fmaf(ry, ry, part);
+      part = fmaf(rz, rz, part);
+    }
+  }
+  return part;
+}
+
+template <int LAYOUT>
 __global__ void __launch_bounds__(256) refine_kernel(const RefineArgs r) {
+  constexpr int U = 4;  // quads in flight per lane
   const int lane = threadIdx.x & 31;
   const int64_t W = (int64_t)gridDim.x * (blockDim.x >> 5);
   const int64_t gw = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -601,39 +689,25 @@ __global__ void __launch_bounds__(256) refine_kernel(const RefineArgs r) {
     const RefineEntry en = r.list[e];
     const float* fr = r.x + en.frame * r.frame_stride;
     CF acc = cf_zero();
-    for (int32_t q = lane; q < Q; q += 32) {
-      float ax[4], ay[4], az[4], bx[4], by[4], bz[4];
-      if (LAYOUT == ATOM_MAJOR) {
-        const float4 t0 = ldg4(fr + 12 * (size_t)q), t1 = ldg4(fr + 12 * (size_t)q + 4),
-                     t2 = ldg4(fr + 12 * (size_t)q + 8);
-        ax[0] = t0.x; ay[0] = t0.y; az[0] = t0.z; ax[1] = t0.w;
-        ay[1] = t1.x; az[1] = t1.y; ax[2] = t1.z; ay[2] = t1.w;
-        az[2] = t2.x; ax[3] = t2.y; ay[3] = t2.z; az[3] = t2.w;
-      } else {
-        const float4 tx = ldg4(fr + 4 * (size_t)q), ty = ldg4(fr + Ap + 4 * (size_t)q),
-                     tz = ldg4(fr + 2 * (size_t)Ap + 4 * (size_t)q);
-        ax[0] = tx.x; ax[1] = tx.y; ax[2] = tx.z; ax[3] = tx.w;
-        ay[0] = ty.x; ay[1] = ty.y; ay[2] = ty.z; ay[3] = ty.w;
-        az[0] = tz.x; az[1] = tz.y; az[2] = tz.z; az[3] = tz.w;
-      }
-      load_ref_quad<LAYOUT, false>(r.ref, Ap, q, bx, by, bz);
-      const int nv = A - 4 * q;
+    int32_t q = lane;
+    for (; q + 32 * (U - 1) < Q; q += 32 * U) {
+      float ax[U][4], ay[U][4], az[U][4];
+#pragma unroll
+      for (int u = 0; u < U; ++u) load_frame_quad<LAYOUT>(fr, Ap, q + 32 * u, ax[u], ay[u], az[u]);
       float part = 0.f;
 #pragma unroll
-      for (int t = 0; t < 4; ++t) {
-        if (t < nv) {
-          const float dx = (ax[t] - en.mu_hi[0]) - en.mu_lo[0];
-          const float dy = (ay[t] - en.mu_hi[1]) - en.mu_lo[1];
-          const float dz = (az[t] - en.mu_hi[2]) - en.mu_lo[2];
-          const float rx = fmaf(en.rot[0], dx, fmaf(en.rot[1], dy, en.rot[2] * dz)) - bx[t];
-          const float ry = fmaf(en.rot[3], dx, fmaf(en.rot[4], dy, en.rot[5] * dz)) - by[t];
-          const float rz = fmaf(en.rot[6], dx, fmaf(en.rot[7], dy, en.rot[8] * dz)) - bz[t];
-          part = fmaf(rx, rx, part);
-          part = fmaf(ry, ry, part);
-          part = fmaf(rz, rz, part);
-        }
+      for (int u = 0; u < U; ++u) {
+        float bx[4], by[4], bz[4];
+        load_ref_quad<LAYOUT, false>(r.ref, Ap, q + 32 * u, bx, by, bz);
+        part += residual_quad(en, ax[u], ay[u], az[u], bx, by, bz, A - 4 * (q + 32 * u));
       }
       cf_add(acc, part);
+    }
+    for (; q < Q; q += 32) {
+      float ax[4], ay[4], az[4], bx[4], by[4], bz[4];
+      load_frame_quad<LAYOUT>(fr, Ap, q, ax, ay, az);
+      load_ref_quad<LAYOUT, false>(r.ref, Ap, q, bx, by, bz);
+      cf_add(acc, residual_quad(en, ax, ay, az, bx, by, bz, A - 4 * q));
     }
 #pragma unroll
     for (int m = 16; m >= 1; m >>= 1) {
@@ -722,29 +796,49 @@ __global__ void __launch_bounds__(256) center_writeback_kernel(float* x, int64_t
 // ---------------------------------------------------------------------------
 
 struct StreamCfg {
+  int warps;
   int cq;
   int nstage;
   bool ref_smem;
 };
 
+// Candidate launch configurations, in order of preference; the first whose
+// shared memory fits is used unless gbrmsd_stream_config_select() forced one.
+constexpr int kNumCfg = 7;
+constexpr StreamCfg kCfgs[kNumCfg] = {
+    {16, 128, 2, true},   // small frames: 2 x 6 KB stages per warp
+    {16, 64, 3, true},    // medium
+    {16, 64, 2, true},    // reference up to ~130 KB in shared memory
+    {16, 64, 4, false},   // reference through L1/L2
+    {8, 128, 3, true},
+    {8, 64, 4, true},
+    {8, 128, 4, false},
+};
+int g_forced_cfg = -1;
+
 size_t stream_smem_bytes(const StreamCfg& c, int32_t Ap, bool use_ref) {
   const size_t ref = (c.ref_smem && use_ref) ? align_up((size_t)Ap * 12, 128) : 0;
-  return ref + (size_t)kWarps * c.nstage * c.cq * 48 + (size_t)kWarps * c.nstage * 8;
+  return ref + (size_t)c.warps * c.nstage * c.cq * 48 + (size_t)c.warps * c.nstage * 8;
+}
+
+bool cfg_fits(const StreamCfg& c, int32_t Ap, bool use_ref) {
+  return stream_smem_bytes(c, Ap, use_ref) <= (size_t)max_dyn_smem();
 }
 
 StreamCfg choose_cfg(int32_t Ap, bool use_ref) {
-  const size_t limit = (size_t)max_dyn_smem();
-  const StreamCfg cands[3] = {{128, 3, true}, {64, 4, true}, {128, 4, false}};
-  for (int i = 0; i < 3; ++i) {
-    if (!use_ref && cands[i].ref_smem) continue;
-    if (stream_smem_bytes(cands[i], Ap, use_ref) <= limit) return cands[i];
+  if (g_forced_cfg >= 0 && cfg_fits(kCfgs[g_forced_cfg], Ap, use_ref)) return kCfgs[g_forced_cfg];
+  for (int i = 0; i < kNumCfg; ++i) {
+    if (!use_ref && kCfgs[i].ref_smem) continue;
+    if (cfg_fits(kCfgs[i], Ap, use_ref)) return kCfgs[i];
   }
-  return cands[2];
+  return kCfgs[3];
 }
 
-int32_t choose_splits(int64_t F, int32_t Q, int grid_warps) {
+int grid_warps(const StreamCfg& c) { return sm_count() * c.warps; }
+
+int32_t choose_splits(int64_t F, int32_t Q, int gwarps) {
   if (F <= 0) return 1;
-  const int64_t target = 16LL * grid_warps;
+  const int64_t target = 16LL * gwarps;
   if (F >= target) return 1;
   int64_t s = (target + F - 1) / F;
   int64_t smax = Q / 32;
@@ -754,21 +848,30 @@ int32_t choose_splits(int64_t F, int32_t Q, int grid_warps) {
   return (int32_t)s;
 }
 
-template <int LAYOUT, int MODE, int CQ, int NSTAGE, bool REF_SMEM>
+template <int LAYOUT, int MODE, int CQ, int NSTAGE, bool REF_SMEM, int WARPS>
 int launch_stream_t(const StreamArgs& a, size_t smem, int grid, cudaStream_t st) {
-  auto k = stream_kernel<LAYOUT, MODE, CQ, NSTAGE, REF_SMEM>;
+  auto k = stream_kernel<LAYOUT, MODE, CQ, NSTAGE, REF_SMEM, WARPS>;
   GB_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
               "cudaFuncSetAttribute(stream_kernel)");
-  k<<<grid, kWarps * 32, smem, st>>>(a);
+  k<<<grid, WARPS * 32, smem, st>>>(a);
   GB_CUDA_TRY(cudaGetLastError(), "launch stream_kernel");
   return GBRMSD_OK;
 }
 
 template <int LAYOUT, int MODE>
 int launch_stream_m(const StreamArgs& a, const StreamCfg& c, size_t smem, int grid, cudaStream_t st) {
-  if (c.cq == 128 && c.nstage == 3 && c.ref_smem) return launch_stream_t<LAYOUT, MODE, 128, 3, true>(a, smem, grid, st);
-  if (c.cq == 64 && c.nstage == 4 && c.ref_smem) return launch_stream_t<LAYOUT, MODE, 64, 4, true>(a, smem, grid, st);
-  return launch_stream_t<LAYOUT, MODE, 128, 4, false>(a, smem, grid, st);
+#define GB_CFG(W, CQ_, NS, RS)                                                   \
+  if (c.warps == W && c.cq == CQ_ && c.nstage == NS && c.ref_smem == RS)        \
+    return launch_stream_t<LAYOUT, MODE, CQ_, NS, RS, W>(a, smem, grid, st);
+  GB_CFG(16, 128, 2, true)
+  GB_CFG(16, 64, 3, true)
+  GB_CFG(16, 64, 2, true)
+  GB_CFG(16, 64, 4, false)
+  GB_CFG(8, 128, 3, true)
+  GB_CFG(8, 64, 4, true)
+  GB_CFG(8, 128, 4, false)
+#undef GB_CFG
+  return set_error(GBRMSD_E_INVALID, "no streaming kernel for this configuration");
 }
 
 template <int LAYOUT>
@@ -781,9 +884,8 @@ int launch_stream_l(int mode, const StreamArgs& a, const StreamCfg& c, size_t sm
   }
 }
 
-int launch_stream(int layout, int mode, const StreamArgs& a, cudaStream_t st) {
+int launch_stream(int layout, int mode, const StreamArgs& a, const StreamCfg& c, cudaStream_t st) {
   const bool use_ref = mode != MODE_TRACE;
-  const StreamCfg c = choose_cfg(a.n_padded, use_ref);
   const size_t smem = stream_smem_bytes(c, a.n_padded, use_ref);
   const int grid = sm_count();
   return layout == ATOM_MAJOR ? launch_stream_l<ATOM_MAJOR>(mode, a, c, smem, grid, st)
@@ -829,8 +931,13 @@ int check_frames(const float* x, int64_t F, int32_t A, int32_t Ap, int64_t frame
 
 }  // namespace
 
-int32_t rmsd_splits(int64_t F, int32_t A) {
-  return choose_splits(F, (A + 3) / 4, sm_count() * kWarps);
+// Splits per frame; mode-independent upper bound so one workspace size
+// serves every mode (TRACE uses the same or fewer splits).
+int32_t rmsd_splits_max(int64_t F, int32_t A) {
+  // the largest split count any configuration could choose for this shape
+  int gw = 0;
+  for (int i = 0; i < kNumCfg; ++i) gw = gw > grid_warps(kCfgs[i]) ? gw : grid_warps(kCfgs[i]);
+  return choose_splits(F, (A + 3) / 4, gw);
 }
 
 // Optional CUDA-event timing of the streaming kernel (the dominant kernel):
@@ -898,7 +1005,7 @@ int gbrmsd_reference_info(const void* ref_ws, float* host_trace, float* host_cen
 
 size_t gbrmsd_rmsd_workspace_bytes(int64_t n_frames, int32_t n_atoms) {
   if (n_frames < 0 || n_atoms < 0) return 0;
-  return ws_layout(n_frames, rmsd_splits(n_frames, n_atoms)).total;
+  return ws_layout(n_frames, rmsd_splits_max(n_frames, n_atoms)).total;
 }
 
 int gbrmsd_rmsd_to_reference(const float* x, int64_t n_frames, int32_t n_atoms, int32_t n_padded,
@@ -923,7 +1030,8 @@ int gbrmsd_rmsd_to_reference(const float* x, int64_t n_frames, int32_t n_atoms, 
     if (out_trace) GB_CUDA_TRY(cudaMemsetAsync(out_trace, 0, sizeof(float) * n_frames, st), "memset");
     return GBRMSD_OK;
   }
-  const int32_t S = rmsd_splits(n_frames, n_atoms);
+  const StreamCfg cfg = choose_cfg(n_padded, true);
+  const int32_t S = choose_splits(n_frames, (n_atoms + 3) / 4, grid_warps(cfg));
   const WsLayout L = ws_layout(n_frames, S);
   if (!ws || ws_bytes < L.total || !aligned16(ws))
     return set_error(GBRMSD_E_WORKSPACE, "rmsd_to_reference: workspace needs %zu bytes (16-byte aligned)", L.total);
@@ -944,7 +1052,7 @@ int gbrmsd_rmsd_to_reference(const float* x, int64_t n_frames, int32_t n_atoms, 
   sa.sums = reinterpret_cast<double*>(w + L.sums_off);
   sa.err = &hdr->err;
   prof_begin(st);
-  rc = launch_stream(layout, mode, sa, st);
+  rc = launch_stream(layout, mode, sa, cfg, st);
   if (rc) return rc;
   prof_end(st);
 
@@ -979,10 +1087,11 @@ int gbrmsd_rmsd_to_reference(const float* x, int64_t n_frames, int32_t n_atoms, 
     ra.list = fa.refine;
     ra.count = fa.refine_count;
     ra.out_rmsd = out_rmsd;
+    const int rgrid = sm_count() * 4;
     if (layout == ATOM_MAJOR)
-      refine_kernel<ATOM_MAJOR><<<sm_count(), 256, 0, st>>>(ra);
+      refine_kernel<ATOM_MAJOR><<<rgrid, 256, 0, st>>>(ra);
     else
-      refine_kernel<AXIS_MAJOR><<<sm_count(), 256, 0, st>>>(ra);
+      refine_kernel<AXIS_MAJOR><<<rgrid, 256, 0, st>>>(ra);
     GB_CUDA_TRY(cudaGetLastError(), "launch refine_kernel");
   }
   return GBRMSD_OK;
@@ -1002,7 +1111,8 @@ int gbrmsd_center_inplace(float* x, int64_t n_frames, int32_t n_atoms, int32_t n
     if (out_centroids) GB_CUDA_TRY(cudaMemsetAsync(out_centroids, 0, sizeof(float) * 3 * n_frames, st), "memset");
     return GBRMSD_OK;
   }
-  const int32_t S = rmsd_splits(n_frames, n_atoms);
+  const StreamCfg cfg = choose_cfg(n_padded, false);
+  const int32_t S = choose_splits(n_frames, (n_atoms + 3) / 4, grid_warps(cfg));
   const WsLayout L = ws_layout(n_frames, S);
   const size_t need = L.total;
   if (!ws || ws_bytes < need || !aligned16(ws))
@@ -1021,7 +1131,7 @@ int gbrmsd_center_inplace(float* x, int64_t n_frames, int32_t n_atoms, int32_t n
   sa.splits = S;
   sa.sums = reinterpret_cast<double*>(w + L.sums_off);
   sa.err = &hdr->err;
-  rc = launch_stream(layout, MODE_TRACE, sa, st);
+  rc = launch_stream(layout, MODE_TRACE, sa, cfg, st);
   if (rc) return rc;
   FinishArgs fa{};
   fa.n_frames = n_frames;
@@ -1041,6 +1151,28 @@ int gbrmsd_center_inplace(float* x, int64_t n_frames, int32_t n_atoms, int32_t n
     center_writeback_kernel<AXIS_MAJOR><<<grid, 256, 0, st>>>(x, n_frames, n_atoms, n_padded, frame_stride, cent, out_traces);
   GB_CUDA_TRY(cudaGetLastError(), "launch center_writeback_kernel");
   return GBRMSD_OK;
+}
+
+int gbrmsd_stream_config_count(void) { return kNumCfg; }
+
+int gbrmsd_stream_config_select(int32_t index) {
+  clear_error();
+  if (index < -1 || index >= kNumCfg)
+    return set_error(GBRMSD_E_INVALID, "stream_config_select: index must be -1 or in [0, %d)", kNumCfg);
+  g_forced_cfg = index;
+  return GBRMSD_OK;
+}
+
+int gbrmsd_stream_config_describe(int32_t index, int32_t n_atoms, int32_t* out4) {
+  clear_error();
+  if (index < 0 || index >= kNumCfg || !out4)
+    return set_error(GBRMSD_E_INVALID, "stream_config_describe: bad arguments");
+  const StreamCfg& c = kCfgs[index];
+  out4[0] = c.warps;
+  out4[1] = c.cq;
+  out4[2] = c.nstage;
+  out4[3] = c.ref_smem ? 1 : 0;
+  return cfg_fits(c, (n_atoms + 3) / 4 * 4, true) ? 1 : 0;
 }
 
 int gbrmsd_profile_enable(int32_t max_calls) {

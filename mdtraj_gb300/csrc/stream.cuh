@@ -16,7 +16,6 @@ enum Mode : int {
   MODE_TRACE = 3,        // exact centroid only (first pass of in-place centring)
 };
 
-constexpr int kWarps = 8;         // warps per CTA of the streaming kernel
 constexpr int SUMS_STRIDE = 20;   // doubles per (frame, split) partial record
 
 // Per-reference information produced by the reference preparation kernel.
