@@ -113,14 +113,15 @@ int gbrmsd_center_inplace(float* x, int64_t n_frames, int32_t n_atoms, int32_t n
 int gbrmsd_workspace_status(const void* ws, void* stream);
 
 /* Launch configurations of the streaming kernel (warps per CTA, quads per
- * stage, stages per warp, reference in shared memory).  By default the first
- * configuration whose shared memory fits is used; select(i) forces
- * configuration i for later calls where it fits (-1 restores the default);
- * used by the tuner.  describe() writes the 4 parameters and returns 1 if the
- * configuration fits frames of n_atoms atoms, 0 if not. */
+ * stage, stages per warp, reference in shared memory, chunks prefetched into
+ * L2 ahead of the stages).  By default the first configuration whose shared
+ * memory fits is used; select(i) forces configuration i for later calls
+ * where it fits (-1 restores the default); used by the tuner.  describe()
+ * writes the 5 parameters and returns 1 if the configuration fits frames of
+ * n_atoms atoms, 0 if not. */
 int gbrmsd_stream_config_count(void);
 int gbrmsd_stream_config_select(int32_t index);
-int gbrmsd_stream_config_describe(int32_t index, int32_t n_atoms, int32_t* out4);
+int gbrmsd_stream_config_describe(int32_t index, int32_t n_atoms, int32_t* out5);
 
 /* Timing of the streaming kernel (the dominant kernel of
  * gbrmsd_rmsd_to_reference) with CUDA events recorded on the caller's stream,
@@ -136,6 +137,28 @@ int gbrmsd_profile_read(float* stream_kernel_ms, int32_t capacity);
  * 1 = host->device, 2 = device->host, 3 = device->device. */
 int gbrmsd_copy_rows(void* dst, size_t dst_pitch, const void* src, size_t src_pitch,
                      size_t row_bytes, size_t n_rows, int32_t kind, void* stream);
+
+/* 1 when kernels on the current device can read and write pageable host
+ * memory through the host page tables (Grace + NVLink-C2C), else 0. */
+int gbrmsd_pageable_access(void);
+
+/* Kernel-based strided row copy: dst row r (dst_pitch floats apart) gets
+ * src row r (src_pitch floats apart, row_floats values), then zeros up to
+ * dst_fill floats.  Either side may be pageable host memory when
+ * gbrmsd_pageable_access() is 1 (unregistered host pointers are refused
+ * otherwise).  Used by the drop-in to move numpy coordinates into the
+ * padded device layout without a staged pageable memcpy. */
+int gbrmsd_copy_rows_kernel(float* dst, int64_t dst_pitch, const float* src, int64_t src_pitch, int64_t row_floats,
+                            int64_t dst_fill, int64_t n_rows, void* stream);
+
+/* The reference's in-place centring side effect (src/center_generic.h:33-38,
+ * x -= (float)centroid in float) written by a kernel straight into the
+ * caller's HOST array (n_frames x n_atoms x 3, unpadded) from the device copy
+ * of the same coordinates (atom-major, dev_frame_stride floats apart) and the
+ * centroids of gbrmsd_rmsd_to_reference.  Needs gbrmsd_pageable_access()
+ * for pageable host memory. */
+int gbrmsd_write_centred(float* host, const float* dev, int64_t dev_frame_stride, const float* centroids,
+                         int64_t n_frames, int32_t n_atoms, void* stream);
 
 /* Host-side replica of the reference's in-place centring side effect
  * (src/center_generic.h:33-38: x -= (float)centroid, in float) on a HOST

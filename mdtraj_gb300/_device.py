@@ -44,23 +44,42 @@ def copy_rows(dst: int, dst_pitch: int, src: int, src_pitch: int, row_bytes: int
     check(lib.gbrmsd_copy_rows(dst, dst_pitch, src, src_pitch, row_bytes, n_rows, kind, stream))
 
 
+_PAGEABLE = None
+
+
+def pageable_access() -> bool:
+    """Kernels can read/write pageable host memory (Grace + NVLink-C2C)."""
+    global _PAGEABLE
+    if _PAGEABLE is None:
+        _PAGEABLE = bool(lib.gbrmsd_pageable_access())
+    return _PAGEABLE
+
+
+def _rows(layout: int, F: int, A: int):
+    """(rows, host row floats, device row floats) of a frame block."""
+    Ap = padded(A)
+    if layout == _lib.ATOM_MAJOR:
+        return F, 3 * A, 3 * Ap
+    return 3 * F, A, Ap
+
+
 def frames_to_device(x: np.ndarray, layout: int, device, stream: int) -> tuple[torch.Tensor, int]:
     """Copies host frames (F, A, 3) atom-major or (F, 3, A) axis-major into a
-    padded, 16-byte aligned device buffer.  Returns (buffer, n_padded)."""
+    padded, 16-byte aligned device buffer (padding atoms zeroed).  Returns
+    (buffer, n_padded).  With pageable host access a kernel reads the numpy
+    memory directly; otherwise a strided cudaMemcpy2DAsync is used."""
     x = np.ascontiguousarray(x, dtype=np.float32)
     F = x.shape[0]
-    if layout == _lib.ATOM_MAJOR:
-        A = x.shape[1]
-        Ap = padded(A)
-        buf = torch.empty((F, Ap * 3), dtype=torch.float32, device=device)
-        if F and A:
-            copy_rows(buf.data_ptr(), Ap * 12, x.ctypes.data, A * 12, A * 12, F, 1, stream)
-    else:
-        A = x.shape[2]
-        Ap = padded(A)
-        buf = torch.empty((F, 3, Ap), dtype=torch.float32, device=device)
-        if F and A:
-            copy_rows(buf.data_ptr(), Ap * 4, x.ctypes.data, A * 4, A * 4, F * 3, 1, stream)
+    A = x.shape[1] if layout == _lib.ATOM_MAJOR else x.shape[2]
+    Ap = padded(A)
+    shape = (F, Ap * 3) if layout == _lib.ATOM_MAJOR else (F, 3, Ap)
+    buf = torch.empty(shape, dtype=torch.float32, device=device)
+    if F and A:
+        rows, hrow, drow = _rows(layout, F, A)
+        if pageable_access():
+            check(lib.gbrmsd_copy_rows_kernel(buf.data_ptr(), drow, x.ctypes.data, hrow, hrow, drow, rows, stream))
+        else:
+            copy_rows(buf.data_ptr(), drow * 4, x.ctypes.data, hrow * 4, hrow * 4, rows, 1, stream)
     return buf, Ap
 
 
@@ -71,10 +90,11 @@ def frames_to_host(buf: torch.Tensor, out: np.ndarray, layout: int, n_atoms: int
     A = int(n_atoms)
     if not F or not A:
         return
-    if layout == _lib.ATOM_MAJOR:
-        copy_rows(out.ctypes.data, A * 12, buf.data_ptr(), n_padded * 12, A * 12, F, 2, stream)
+    rows, hrow, drow = _rows(layout, F, A)
+    if pageable_access():
+        check(lib.gbrmsd_copy_rows_kernel(out.ctypes.data, hrow, buf.data_ptr(), drow, hrow, hrow, rows, stream))
     else:
-        copy_rows(out.ctypes.data, A * 4, buf.data_ptr(), n_padded * 4, A * 4, F * 3, 2, stream)
+        copy_rows(out.ctypes.data, hrow * 4, buf.data_ptr(), drow * 4, hrow * 4, rows, 2, stream)
 
 
 def to_host(t: torch.Tensor, stream: int) -> np.ndarray:

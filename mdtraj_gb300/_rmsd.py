@@ -177,11 +177,18 @@ def rmsd(target, reference, frame=0, atom_indices=None, ref_atom_indices=None, p
         cent = torch.empty((n_frames, 3), dtype=torch.float32, device=device) if mutate_target else None
         D.rmsd_to_reference(x_dev, n_frames, n_atoms, n_padded, _lib.ATOM_MAJOR, _lib.MODE_CENTER, ref,
                             self_index=self_index, out=out, centroid_out=cent)
-        result = D.to_host(out, stream)
-        if mutate_target:
-            cent_h = D.to_host(cent, stream)
-            check(lib.gbrmsd_host_subtract_centroids(target_xyz.ctypes.data, n_frames, n_atoms, 3 * n_atoms,
-                                                     cent_h.ctypes.data, 0))
+        if mutate_target and D.pageable_access():
+            # the reference centres target.xyz in place: written back by a
+            # kernel from the device copy, straight into the numpy array
+            check(lib.gbrmsd_write_centred(target_xyz.ctypes.data, x_dev.data_ptr(), 3 * n_padded,
+                                           cent.data_ptr(), n_frames, n_atoms, stream))
+            result = D.to_host(out, stream)
+        else:
+            result = D.to_host(out, stream)
+            if mutate_target:
+                cent_h = D.to_host(cent, stream)
+                check(lib.gbrmsd_host_subtract_centroids(target_xyz.ctypes.data, n_frames, n_atoms,
+                                                         3 * n_atoms, cent_h.ctypes.data, 0))
         if mutate_ref:
             _centre_frame_like_reference(ref_xyz_frame, ref)
         return result

@@ -137,6 +137,12 @@ GB_DEV void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) 
       : "memory");
 }
 
+// Bulk prefetch of [src, src + bytes) into L2 (no shared memory, no
+// completion tracking).  src 16-byte aligned, bytes a multiple of 16.
+GB_DEV void bulk_prefetch_l2(const void* src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
+
 GB_DEV bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   uint32_t ok;
   asm volatile(

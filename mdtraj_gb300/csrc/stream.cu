@@ -206,6 +206,20 @@ __device__ __forceinline__ void issue_chunk(const StreamArgs& p, const Cursor& c
   }
 }
 
+// L2 prefetch of the chunk at `cur` (same byte ranges as issue_chunk).
+template <int LAYOUT, int CQ>
+__device__ __forceinline__ void prefetch_chunk(const StreamArgs& p, const Cursor& cur) {
+  const int32_t qb = cur.q0 + cur.c * CQ;
+  const int32_t nq = min(CQ, cur.q1 - qb);
+  const float* fbase = p.x + cur.frame * p.frame_stride;
+  if (LAYOUT == ATOM_MAJOR) {
+    bulk_prefetch_l2(fbase + (size_t)qb * 12, (uint32_t)nq * 48u);
+  } else {
+#pragma unroll
+    for (int r = 0; r < 3; ++r) bulk_prefetch_l2(fbase + (size_t)r * p.n_padded + (size_t)qb * 4, (uint32_t)nq * 16u);
+  }
+}
+
 // Loads quad i of a stage (or of the reference) as x[4], y[4], z[4].
 template <int LAYOUT, int CQ>
 __device__ __forceinline__ void load_stage_quad(const float* st, int i, float (&x)[4], float (&y)[4],
@@ -303,7 +317,7 @@ __device__ __forceinline__ void accum_quad(float (&acc)[NV], const float (&ax)[4
 // issues NSTAGE chunks ahead.  FP32 level-1 sums cover at most 4 quads per
 // lane (16 atoms) before they are folded into TwoSum pairs, which bounds the
 // rounding error of the one-pass sums independently of the atom count.
-template <int LAYOUT, int MODE, int CQ, int NSTAGE, bool REF_SMEM, int WARPS>
+template <int LAYOUT, int MODE, int CQ, int NSTAGE, bool REF_SMEM, int WARPS, int PF>
 __global__ void __launch_bounds__(WARPS * 32, 1) stream_kernel(const StreamArgs p) {
   extern __shared__ __align__(128) unsigned char smem[];
   constexpr int STAGE_BYTES = CQ * 48;
@@ -340,10 +354,23 @@ __global__ void __launch_bounds__(WARPS * 32, 1) stream_kernel(const StreamArgs 
   const int64_t W = (int64_t)gridDim.x * WARPS;
   const int64_t gw = (int64_t)blockIdx.x * WARPS + warp;
 
-  Cursor pc, cc;
+  // Cursors: consumer (cc), bulk copies into shared memory (pc, NSTAGE ahead)
+  // and, when PF > 0, L2 prefetches (fc, NSTAGE + PF ahead) that hide HBM
+  // latency without holding shared memory.
+  Cursor pc, cc, fc;
   cursor_unit<CQ>(pc, gw, S, Q);
   cursor_unit<CQ>(cc, gw, S, Q);
+  cursor_unit<CQ>(fc, gw, S, Q);
   int64_t issued = 0, consumed = 0;
+  if constexpr (PF > 0) {
+#pragma unroll 1
+    for (int s = 0; s < NSTAGE + PF; ++s) {
+      if (fc.unit < n_units) {
+        if (lane == 0) prefetch_chunk<LAYOUT, CQ>(p, fc);
+        cursor_next<CQ>(fc, W, S, Q);
+      }
+    }
+  }
 #pragma unroll 1
   for (int s = 0; s < NSTAGE; ++s) {
     if (pc.unit < n_units) {
@@ -448,6 +475,12 @@ __global__ void __launch_bounds__(WARPS * 32, 1) stream_kernel(const StreamArgs 
       }
       cursor_next<CQ>(pc, W, S, Q);
       ++issued;
+    }
+    if constexpr (PF > 0) {
+      if (fc.unit < n_units) {
+        if (lane == 0) prefetch_chunk<LAYOUT, CQ>(p, fc);
+        cursor_next<CQ>(fc, W, S, Q);
+      }
     }
     slot = (slot + 1 == NSTAGE) ? 0 : slot + 1;
 
@@ -597,16 +630,16 @@ __global__ void __launch_bounds__(256) finish_kernel(const FinishArgs a) {
     return;
   }
   int iters = 0;
-  const double lam = qcp_lambda_max(m, ga, gb, &iters);
+  const double lam = qcp_lambda_max_mixed(m, ga, gb, &iters);
   double msd = (ga + gb - 2.0 * lam) / dA;
   if (!(msd > 0.0)) msd = 0.0;
-  a.out_rmsd[f] = (float)sqrt(msd);
+  a.out_rmsd[f] = sqrtf((float)msd);
 
-  // One-pass sums resolve msd to about 1e-7 * scale / sqrt(A); below the
-  // threshold the direct residual is recomputed (see refine_kernel).
+  // One-pass sums resolve msd to about 1e-7 * scale / sqrt(A); below
+  // (0.1 * scale / sqrt(A))^2 the direct residual is recomputed (see
+  // refine_kernel).  scale = (G_a + G_b) / (2 A).
   const double scale = (ga + gb) / (2.0 * dA);
-  const double thr = 0.1 * scale / sqrt(dA);
-  if (msd < thr * thr && A > 0) {
+  if (msd * dA < 0.01 * scale * scale && A > 0) {
     double rot[9];
     qcp_rotation(m, lam, rot);
     const int slot = atomicAdd(a.refine_count, 1);
@@ -800,19 +833,22 @@ struct StreamCfg {
   int cq;
   int nstage;
   bool ref_smem;
+  int pf;  // chunks prefetched into L2 beyond the shared-memory stages
 };
 
 // Candidate launch configurations, in order of preference; the first whose
 // shared memory fits is used unless gbrmsd_stream_config_select() forced one.
-constexpr int kNumCfg = 7;
+constexpr int kNumCfg = 9;
 constexpr StreamCfg kCfgs[kNumCfg] = {
-    {16, 128, 2, true},   // small frames: 2 x 6 KB stages per warp
-    {16, 64, 3, true},    // medium
-    {16, 64, 2, true},    // reference up to ~130 KB in shared memory
-    {16, 64, 4, false},   // reference through L1/L2
-    {8, 128, 3, true},
-    {8, 64, 4, true},
-    {8, 128, 4, false},
+    {16, 128, 2, true, 0},   // small frames: 2 x 6 KB stages per warp
+    {16, 64, 2, true, 8},    // reference up to ~130 KB in shared memory, L2 prefetch 8 chunks ahead
+    {16, 64, 2, true, 0},
+    {16, 64, 3, true, 4},
+    {16, 128, 2, true, 4},
+    {16, 64, 4, false, 4},   // reference through L1/L2
+    {8, 64, 4, true, 8},
+    {16, 64, 2, true, 16},
+    {8, 128, 4, false, 0},
 };
 int g_forced_cfg = -1;
 
@@ -831,7 +867,7 @@ StreamCfg choose_cfg(int32_t Ap, bool use_ref) {
     if (!use_ref && kCfgs[i].ref_smem) continue;
     if (cfg_fits(kCfgs[i], Ap, use_ref)) return kCfgs[i];
   }
-  return kCfgs[3];
+  return kCfgs[8];
 }
 
 int grid_warps(const StreamCfg& c) { return sm_count() * c.warps; }
@@ -848,9 +884,9 @@ int32_t choose_splits(int64_t F, int32_t Q, int gwarps) {
   return (int32_t)s;
 }
 
-template <int LAYOUT, int MODE, int CQ, int NSTAGE, bool REF_SMEM, int WARPS>
+template <int LAYOUT, int MODE, int CQ, int NSTAGE, bool REF_SMEM, int WARPS, int PF>
 int launch_stream_t(const StreamArgs& a, size_t smem, int grid, cudaStream_t st) {
-  auto k = stream_kernel<LAYOUT, MODE, CQ, NSTAGE, REF_SMEM, WARPS>;
+  auto k = stream_kernel<LAYOUT, MODE, CQ, NSTAGE, REF_SMEM, WARPS, PF>;
   GB_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
               "cudaFuncSetAttribute(stream_kernel)");
   k<<<grid, WARPS * 32, smem, st>>>(a);
@@ -860,16 +896,18 @@ int launch_stream_t(const StreamArgs& a, size_t smem, int grid, cudaStream_t st)
 
 template <int LAYOUT, int MODE>
 int launch_stream_m(const StreamArgs& a, const StreamCfg& c, size_t smem, int grid, cudaStream_t st) {
-#define GB_CFG(W, CQ_, NS, RS)                                                   \
-  if (c.warps == W && c.cq == CQ_ && c.nstage == NS && c.ref_smem == RS)        \
-    return launch_stream_t<LAYOUT, MODE, CQ_, NS, RS, W>(a, smem, grid, st);
-  GB_CFG(16, 128, 2, true)
-  GB_CFG(16, 64, 3, true)
-  GB_CFG(16, 64, 2, true)
-  GB_CFG(16, 64, 4, false)
-  GB_CFG(8, 128, 3, true)
-  GB_CFG(8, 64, 4, true)
-  GB_CFG(8, 128, 4, false)
+#define GB_CFG(W, CQ_, NS, RS, PF_)                                                        \
+  if (c.warps == W && c.cq == CQ_ && c.nstage == NS && c.ref_smem == RS && c.pf == PF_) \
+    return launch_stream_t<LAYOUT, MODE, CQ_, NS, RS, W, PF_>(a, smem, grid, st);
+  GB_CFG(16, 128, 2, true, 0)
+  GB_CFG(16, 64, 2, true, 8)
+  GB_CFG(16, 64, 2, true, 0)
+  GB_CFG(16, 64, 3, true, 4)
+  GB_CFG(16, 128, 2, true, 4)
+  GB_CFG(16, 64, 4, false, 4)
+  GB_CFG(8, 64, 4, true, 8)
+  GB_CFG(16, 64, 2, true, 16)
+  GB_CFG(8, 128, 4, false, 0)
 #undef GB_CFG
   return set_error(GBRMSD_E_INVALID, "no streaming kernel for this configuration");
 }
@@ -1163,7 +1201,8 @@ int gbrmsd_stream_config_select(int32_t index) {
   return GBRMSD_OK;
 }
 
-int gbrmsd_stream_config_describe(int32_t index, int32_t n_atoms, int32_t* out4) {
+int gbrmsd_stream_config_describe(int32_t index, int32_t n_atoms, int32_t* out5) {
+  int32_t* out4 = out5;
   clear_error();
   if (index < 0 || index >= kNumCfg || !out4)
     return set_error(GBRMSD_E_INVALID, "stream_config_describe: bad arguments");
@@ -1172,6 +1211,7 @@ int gbrmsd_stream_config_describe(int32_t index, int32_t n_atoms, int32_t* out4)
   out4[1] = c.cq;
   out4[2] = c.nstage;
   out4[3] = c.ref_smem ? 1 : 0;
+  out4[4] = c.pf;
   return cfg_fits(c, (n_atoms + 3) / 4 * 4, true) ? 1 : 0;
 }
 
