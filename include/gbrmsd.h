@@ -113,8 +113,7 @@ int gbrmsd_center_inplace(float* x, int64_t n_frames, int32_t n_atoms, int32_t n
 int gbrmsd_workspace_status(const void* ws, void* stream);
 
 /* Launch configurations of the streaming kernel (warps per CTA, quads per
- * stage, stages per warp, reference in shared memory, chunks prefetched into
- * L2 ahead of the stages).  By default the first configuration whose shared
+ * stage, stages per warp, reference in shared memory, reserved = 0).  By default the first configuration whose shared
  * memory fits is used; select(i) forces configuration i for later calls
  * where it fits (-1 restores the default); used by the tuner.  describe()
  * writes the 5 parameters and returns 1 if the configuration fits frames of

@@ -177,3 +177,90 @@ def center_inplace(x: torch.Tensor, n_frames: int, n_atoms: int, n_padded: int, 
     check(lib.gbrmsd_center_inplace(ptr(x), n_frames, n_atoms, n_padded, 3 * n_padded, layout,
                                     ptr(traces_out), ptr(centroid_out), ws.data_ptr(), ws.numel(), stream))
     return traces_out
+
+
+# ---------------------------------------------------------------------------
+# Pipelined host-buffer path
+# ---------------------------------------------------------------------------
+
+_STREAMS: dict = {}
+
+
+def _side_streams(device) -> tuple[torch.cuda.Stream, torch.cuda.Stream]:
+    key = (device.type, device.index)
+    if key not in _STREAMS:
+        _STREAMS[key] = (torch.cuda.Stream(device=device), torch.cuda.Stream(device=device))
+    return _STREAMS[key]
+
+
+def rmsd_host_frames(x: np.ndarray, ref: "DeviceReference", mode: int, *, g_target: np.ndarray | None = None,
+                     g_ref: float = 0.0, self_index: int = -1, write_centred: bool = False,
+                     chunk_bytes: int = 256 << 20, ring: int = 3) -> np.ndarray:
+    """RMSD of every frame of a HOST atom-major array (F, A, 3) float32 to a
+    prepared reference, streamed through the GPU in chunks.
+
+    Chunk k's host->device copy (stream 1) overlaps the kernels and, with
+    `write_centred`, the in-place centring write-back of chunk k-1 (stream 2),
+    so the two directions of the host link run concurrently.  A ring of
+    `ring` device chunk buffers bounds device memory.  Returns float32 (F,).
+    """
+    device = require_device()
+    F, A = x.shape[0], x.shape[1]
+    Ap = padded(A)
+    frame_bytes = 12 * max(A, 1)
+    C = max(1, min(F, chunk_bytes // frame_bytes))
+    n_chunks = (F + C - 1) // C
+    s_in, s_work = _side_streams(device)
+    cur = torch.cuda.current_stream(device)
+    out = torch.empty(F, dtype=torch.float32, device=device)
+    cent = torch.empty((F, 3), dtype=torch.float32, device=device) if write_centred else None
+    g_dev = torch.from_numpy(np.ascontiguousarray(g_target, dtype=np.float32)).to(device) \
+        if g_target is not None else None
+    bufs = [torch.empty((C, 3 * Ap), dtype=torch.float32, device=device) for _ in range(min(ring, n_chunks))]
+    ws = empty_bytes(lib.gbrmsd_rmsd_workspace_bytes(C, A), device)
+    host_ok = pageable_access()
+    in_done = [torch.cuda.Event() for _ in range(n_chunks)]
+    work_done = [torch.cuda.Event() for _ in range(n_chunks)]
+    s_in.wait_stream(cur)
+    s_work.wait_stream(cur)
+    for k in range(n_chunks):
+        f0 = k * C
+        n = min(C, F - f0)
+        buf = bufs[k % len(bufs)]
+        src = x.ctypes.data + f0 * 12 * A
+        with torch.cuda.stream(s_in):
+            if k >= len(bufs):
+                s_in.wait_event(work_done[k - len(bufs)])
+            if host_ok:
+                check(lib.gbrmsd_copy_rows_kernel(buf.data_ptr(), 3 * Ap, src, 3 * A, 3 * A, 3 * Ap, n,
+                                                  s_in.cuda_stream))
+            else:
+                copy_rows(buf.data_ptr(), 12 * Ap, src, 12 * A, 12 * A, n, 1, s_in.cuda_stream)
+            in_done[k].record(s_in)
+        with torch.cuda.stream(s_work):
+            s_work.wait_event(in_done[k])
+            si = self_index - f0 if 0 <= self_index - f0 < n else -1
+            check(lib.gbrmsd_rmsd_to_reference(
+                buf.data_ptr(), n, A, Ap, 3 * Ap, _lib.ATOM_MAJOR, mode, ref.ws.data_ptr(),
+                ptr(g_dev[f0:f0 + n]) if g_dev is not None else None, float(g_ref), si,
+                out[f0:f0 + n].data_ptr(), cent[f0:f0 + n].data_ptr() if cent is not None else None, None,
+                ws.data_ptr(), ws.numel(), s_work.cuda_stream))
+            if write_centred:
+                dst = x.ctypes.data + f0 * 12 * A
+                if host_ok:
+                    check(lib.gbrmsd_write_centred(dst, buf.data_ptr(), 3 * Ap, cent[f0:f0 + n].data_ptr(), n, A,
+                                                   s_work.cuda_stream))
+            work_done[k].record(s_work)
+    result = np.empty(F, dtype=np.float32)
+    copy_rows(result.ctypes.data, 4 * F, out.data_ptr(), 4 * F, 4 * F, 1, 2, s_work.cuda_stream)
+    s_work.synchronize()
+    s_in.synchronize()
+    if write_centred and not host_ok:
+        cent_h = np.empty((F, 3), dtype=np.float32)
+        copy_rows(cent_h.ctypes.data, cent_h.nbytes, cent.data_ptr(), cent_h.nbytes, cent_h.nbytes, 1, 2,
+                  s_work.cuda_stream)
+        s_work.synchronize()
+        check(lib.gbrmsd_host_subtract_centroids(x.ctypes.data, F, A, 3 * A, cent_h.ctypes.data, 0))
+    # keep the device buffers alive until both streams are done
+    del bufs, ws, out, cent, g_dev
+    return result

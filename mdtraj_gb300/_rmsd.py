@@ -156,47 +156,28 @@ def rmsd(target, reference, frame=0, atom_indices=None, ref_atom_indices=None, p
         mode = _lib.MODE_NOSUPERPOSE
 
     device = D.require_device()
-    stream = D.stream_handle()
-    x_dev, n_padded = D.frames_to_device(target_xyz, _lib.ATOM_MAJOR, device, stream)
-    out = torch.empty(n_frames, dtype=torch.float32, device=device)
     self_index = _alias_index(target_xyz, ref_xyz_frame)
 
     if mode == _lib.MODE_PRECENTERED:
         target_g = np.ascontiguousarray(target._rmsd_traces, dtype=np.float32)
         ref_g = np.float32(reference._rmsd_traces[frame])
-        g_dev = torch.from_numpy(target_g).to(device)
         ref = D.DeviceReference(ref_xyz_frame, _lib.ATOM_MAJOR, centre=False, device=device)
-        D.rmsd_to_reference(x_dev, n_frames, n_atoms, n_padded, _lib.ATOM_MAJOR, _lib.MODE_PRECENTERED, ref,
-                            g_target=g_dev, g_ref=float(ref_g), self_index=self_index, out=out)
-        return D.to_host(out, stream)
+        return D.rmsd_host_frames(target_xyz, ref, _lib.MODE_PRECENTERED, g_target=target_g[:n_frames],
+                                  g_ref=float(ref_g), self_index=self_index)
 
     if mode == _lib.MODE_CENTER:
         ref = D.DeviceReference(ref_xyz_frame, _lib.ATOM_MAJOR, centre=True, device=device)
+        # the reference centres target.xyz in place when it is a view of it
         mutate_target = n_atoms > 0 and np.may_share_memory(target_xyz, target.xyz)
         mutate_ref = n_atoms > 0 and np.may_share_memory(ref_xyz_frame, reference.xyz)
-        cent = torch.empty((n_frames, 3), dtype=torch.float32, device=device) if mutate_target else None
-        D.rmsd_to_reference(x_dev, n_frames, n_atoms, n_padded, _lib.ATOM_MAJOR, _lib.MODE_CENTER, ref,
-                            self_index=self_index, out=out, centroid_out=cent)
-        if mutate_target and D.pageable_access():
-            # the reference centres target.xyz in place: written back by a
-            # kernel from the device copy, straight into the numpy array
-            check(lib.gbrmsd_write_centred(target_xyz.ctypes.data, x_dev.data_ptr(), 3 * n_padded,
-                                           cent.data_ptr(), n_frames, n_atoms, stream))
-            result = D.to_host(out, stream)
-        else:
-            result = D.to_host(out, stream)
-            if mutate_target:
-                cent_h = D.to_host(cent, stream)
-                check(lib.gbrmsd_host_subtract_centroids(target_xyz.ctypes.data, n_frames, n_atoms,
-                                                         3 * n_atoms, cent_h.ctypes.data, 0))
+        result = D.rmsd_host_frames(target_xyz, ref, _lib.MODE_CENTER, self_index=self_index,
+                                    write_centred=mutate_target)
         if mutate_ref:
             _centre_frame_like_reference(ref_xyz_frame, ref)
         return result
 
     ref = D.DeviceReference(ref_xyz_frame, _lib.ATOM_MAJOR, centre=False, device=device)
-    D.rmsd_to_reference(x_dev, n_frames, n_atoms, n_padded, _lib.ATOM_MAJOR, _lib.MODE_NOSUPERPOSE, ref,
-                        self_index=-1, out=out)
-    return D.to_host(out, stream)
+    return D.rmsd_host_frames(target_xyz, ref, _lib.MODE_NOSUPERPOSE)
 
 
 def _centre_frame_like_reference(frame_xyz: np.ndarray, ref: D.DeviceReference) -> None:

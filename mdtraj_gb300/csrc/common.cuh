@@ -137,10 +137,15 @@ GB_DEV void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) 
       : "memory");
 }
 
-// Bulk prefetch of [src, src + bytes) into L2 (no shared memory, no
-// completion tracking).  src 16-byte aligned, bytes a multiple of 16.
-GB_DEV void bulk_prefetch_l2(const void* src, uint32_t bytes) {
-  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+// 3-D tiled tensor copy global -> shared (TMA), completion on `bar`.  The
+// tensor map lives in kernel parameter space (__grid_constant__).  The
+// innermost coordinate x times the element size must be a multiple of 16.
+GB_DEV void tma_load_3d(void* dst, const void* tmap, int32_t x, int32_t y, int32_t z, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];" ::"r"(smem_addr(dst)),
+      "l"(tmap), "r"(x), "r"(y), "r"(z), "r"(smem_addr(bar))
+      : "memory");
 }
 
 GB_DEV bool mbar_try_wait(uint64_t* bar, uint32_t parity) {

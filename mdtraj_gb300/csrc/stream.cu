@@ -27,7 +27,9 @@
 // msd_atom_major per frame), src/center_generic.h:3-44 (centring),
 // src/theobald_rmsd_generic.h:7-119 (3x3 inner products),
 // src/theobald_rmsd.cpp:217-334 (QCP).
+#include <cuda.h>
 #include <math.h>
+#include <string.h>
 
 #include "capi_internal.h"
 #include "common.cuh"
@@ -189,34 +191,26 @@ __device__ __forceinline__ bool cursor_next(Cursor& cur, int64_t W, int32_t S, i
   return false;
 }
 
+// Axis-major stages are a sequence of 64-quad boxes [x 256 | y 256 | z 256]
+// (3 KB), each moved by one 3-D tensor copy of the box (256 atoms, 3 axes, 1
+// frame); atom-major stages are one contiguous 1-D bulk copy.
+constexpr int BOX_QUADS = 64;
+constexpr int BOX_BYTES = BOX_QUADS * 48;
+
 template <int LAYOUT, int CQ>
-__device__ __forceinline__ void issue_chunk(const StreamArgs& p, const Cursor& cur,
+__device__ __forceinline__ void issue_chunk(const StreamArgs& p, const void* tmap, const Cursor& cur,
                                             unsigned char* stage, uint64_t* bar) {
   const int32_t qb = cur.q0 + cur.c * CQ;
   const int32_t nq = min(CQ, cur.q1 - qb);
-  const float* fbase = p.x + cur.frame * p.frame_stride;
-  mbar_arrive_expect_tx(bar, (uint32_t)nq * 48u);
   if (LAYOUT == ATOM_MAJOR) {
+    const float* fbase = p.x + cur.frame * p.frame_stride;
+    mbar_arrive_expect_tx(bar, (uint32_t)nq * 48u);
     bulk_g2s(stage, fbase + (size_t)qb * 12, (uint32_t)nq * 48u, bar);
   } else {
-#pragma unroll
-    for (int r = 0; r < 3; ++r)
-      bulk_g2s(stage + r * CQ * 16, fbase + (size_t)r * p.n_padded + (size_t)qb * 4,
-               (uint32_t)nq * 16u, bar);
-  }
-}
-
-// L2 prefetch of the chunk at `cur` (same byte ranges as issue_chunk).
-template <int LAYOUT, int CQ>
-__device__ __forceinline__ void prefetch_chunk(const StreamArgs& p, const Cursor& cur) {
-  const int32_t qb = cur.q0 + cur.c * CQ;
-  const int32_t nq = min(CQ, cur.q1 - qb);
-  const float* fbase = p.x + cur.frame * p.frame_stride;
-  if (LAYOUT == ATOM_MAJOR) {
-    bulk_prefetch_l2(fbase + (size_t)qb * 12, (uint32_t)nq * 48u);
-  } else {
-#pragma unroll
-    for (int r = 0; r < 3; ++r) bulk_prefetch_l2(fbase + (size_t)r * p.n_padded + (size_t)qb * 4, (uint32_t)nq * 16u);
+    const int nbox = (nq + BOX_QUADS - 1) / BOX_QUADS;
+    mbar_arrive_expect_tx(bar, (uint32_t)(nbox * BOX_BYTES));
+    for (int b = 0; b < nbox; ++b)
+      tma_load_3d(stage + b * BOX_BYTES, tmap, 4 * (qb + b * BOX_QUADS), 0, (int32_t)cur.frame, bar);
   }
 }
 
@@ -230,8 +224,8 @@ __device__ __forceinline__ void load_stage_quad(const float* st, int i, float (&
     y[1] = t1.x; z[1] = t1.y; x[2] = t1.z; y[2] = t1.w;
     z[2] = t2.x; x[3] = t2.y; y[3] = t2.z; z[3] = t2.w;
   } else {
-    const float4 tx = lds4(st + 4 * i), ty = lds4(st + CQ * 4 + 4 * i),
-                 tz = lds4(st + 2 * CQ * 4 + 4 * i);
+    const float* b = st + (i / BOX_QUADS) * (BOX_BYTES / 4) + 4 * (i % BOX_QUADS);
+    const float4 tx = lds4(b), ty = lds4(b + 4 * BOX_QUADS), tz = lds4(b + 8 * BOX_QUADS);
     x[0] = tx.x; x[1] = tx.y; x[2] = tx.z; x[3] = tx.w;
     y[0] = ty.x; y[1] = ty.y; y[2] = ty.z; y[3] = ty.w;
     z[0] = tz.x; z[1] = tz.y; z[2] = tz.z; z[3] = tz.w;
@@ -317,8 +311,9 @@ __device__ __forceinline__ void accum_quad(float (&acc)[NV], const float (&ax)[4
 // issues NSTAGE chunks ahead.  FP32 level-1 sums cover at most 4 quads per
 // lane (16 atoms) before they are folded into TwoSum pairs, which bounds the
 // rounding error of the one-pass sums independently of the atom count.
-template <int LAYOUT, int MODE, int CQ, int NSTAGE, bool REF_SMEM, int WARPS, int PF>
-__global__ void __launch_bounds__(WARPS * 32, 1) stream_kernel(const StreamArgs p) {
+template <int LAYOUT, int MODE, int CQ, int NSTAGE, bool REF_SMEM, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32, 1) stream_kernel(const StreamArgs p,
+                                                               const __grid_constant__ CUtensorMap tmap) {
   extern __shared__ __align__(128) unsigned char smem[];
   constexpr int STAGE_BYTES = CQ * 48;
   constexpr int NV = NSums<MODE>::value;
@@ -354,27 +349,17 @@ __global__ void __launch_bounds__(WARPS * 32, 1) stream_kernel(const StreamArgs 
   const int64_t W = (int64_t)gridDim.x * WARPS;
   const int64_t gw = (int64_t)blockIdx.x * WARPS + warp;
 
-  // Cursors: consumer (cc), bulk copies into shared memory (pc, NSTAGE ahead)
-  // and, when PF > 0, L2 prefetches (fc, NSTAGE + PF ahead) that hide HBM
-  // latency without holding shared memory.
-  Cursor pc, cc, fc;
+  // Cursors: consumer (cc) and bulk copies into shared memory (pc, NSTAGE
+  // chunks ahead).
+  const void* tm = &tmap;
+  Cursor pc, cc;
   cursor_unit<CQ>(pc, gw, S, Q);
   cursor_unit<CQ>(cc, gw, S, Q);
-  cursor_unit<CQ>(fc, gw, S, Q);
   int64_t issued = 0, consumed = 0;
-  if constexpr (PF > 0) {
-#pragma unroll 1
-    for (int s = 0; s < NSTAGE + PF; ++s) {
-      if (fc.unit < n_units) {
-        if (lane == 0) prefetch_chunk<LAYOUT, CQ>(p, fc);
-        cursor_next<CQ>(fc, W, S, Q);
-      }
-    }
-  }
 #pragma unroll 1
   for (int s = 0; s < NSTAGE; ++s) {
     if (pc.unit < n_units) {
-      if (lane == 0) issue_chunk<LAYOUT, CQ>(p, pc, stages + s * STAGE_BYTES, &bars[s]);
+      if (lane == 0) issue_chunk<LAYOUT, CQ>(p, tm, pc, stages + s * STAGE_BYTES, &bars[s]);
       cursor_next<CQ>(pc, W, S, Q);
       ++issued;
     }
@@ -471,16 +456,10 @@ __global__ void __launch_bounds__(WARPS * 32, 1) stream_kernel(const StreamArgs 
     if (pc.unit < n_units) {
       if (lane == 0) {
         fence_proxy_async_smem();
-        issue_chunk<LAYOUT, CQ>(p, pc, stages + slot * STAGE_BYTES, &bars[slot]);
+        issue_chunk<LAYOUT, CQ>(p, tm, pc, stages + slot * STAGE_BYTES, &bars[slot]);
       }
       cursor_next<CQ>(pc, W, S, Q);
       ++issued;
-    }
-    if constexpr (PF > 0) {
-      if (fc.unit < n_units) {
-        if (lane == 0) prefetch_chunk<LAYOUT, CQ>(p, fc);
-        cursor_next<CQ>(fc, W, S, Q);
-      }
     }
     slot = (slot + 1 == NSTAGE) ? 0 : slot + 1;
 
@@ -833,22 +812,19 @@ struct StreamCfg {
   int cq;
   int nstage;
   bool ref_smem;
-  int pf;  // chunks prefetched into L2 beyond the shared-memory stages
 };
 
 // Candidate launch configurations, in order of preference; the first whose
 // shared memory fits is used unless gbrmsd_stream_config_select() forced one.
-constexpr int kNumCfg = 9;
+constexpr int kNumCfg = 7;
 constexpr StreamCfg kCfgs[kNumCfg] = {
-    {16, 128, 2, true, 0},   // small frames: 2 x 6 KB stages per warp
-    {16, 64, 2, true, 8},    // reference up to ~130 KB in shared memory, L2 prefetch 8 chunks ahead
-    {16, 64, 2, true, 0},
-    {16, 64, 3, true, 4},
-    {16, 128, 2, true, 4},
-    {16, 64, 4, false, 4},   // reference through L1/L2
-    {8, 64, 4, true, 8},
-    {16, 64, 2, true, 16},
-    {8, 128, 4, false, 0},
+    {16, 128, 2, true},   // small frames: 2 x 6 KB stages per warp
+    {16, 64, 3, true},    // medium frames
+    {16, 64, 2, true},    // reference up to ~130 KB in shared memory
+    {16, 64, 4, false},   // reference through L1/L2
+    {8, 128, 3, true},
+    {8, 64, 4, true},
+    {8, 128, 4, false},
 };
 int g_forced_cfg = -1;
 
@@ -867,7 +843,7 @@ StreamCfg choose_cfg(int32_t Ap, bool use_ref) {
     if (!use_ref && kCfgs[i].ref_smem) continue;
     if (cfg_fits(kCfgs[i], Ap, use_ref)) return kCfgs[i];
   }
-  return kCfgs[8];
+  return kCfgs[6];
 }
 
 int grid_warps(const StreamCfg& c) { return sm_count() * c.warps; }
@@ -884,50 +860,85 @@ int32_t choose_splits(int64_t F, int32_t Q, int gwarps) {
   return (int32_t)s;
 }
 
-template <int LAYOUT, int MODE, int CQ, int NSTAGE, bool REF_SMEM, int WARPS, int PF>
-int launch_stream_t(const StreamArgs& a, size_t smem, int grid, cudaStream_t st) {
-  auto k = stream_kernel<LAYOUT, MODE, CQ, NSTAGE, REF_SMEM, WARPS, PF>;
+template <int LAYOUT, int MODE, int CQ, int NSTAGE, bool REF_SMEM, int WARPS>
+int launch_stream_t(const StreamArgs& a, const CUtensorMap& tmap, size_t smem, int grid, cudaStream_t st) {
+  auto k = stream_kernel<LAYOUT, MODE, CQ, NSTAGE, REF_SMEM, WARPS>;
   GB_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
               "cudaFuncSetAttribute(stream_kernel)");
-  k<<<grid, WARPS * 32, smem, st>>>(a);
+  k<<<grid, WARPS * 32, smem, st>>>(a, tmap);
   GB_CUDA_TRY(cudaGetLastError(), "launch stream_kernel");
   return GBRMSD_OK;
 }
 
 template <int LAYOUT, int MODE>
-int launch_stream_m(const StreamArgs& a, const StreamCfg& c, size_t smem, int grid, cudaStream_t st) {
-#define GB_CFG(W, CQ_, NS, RS, PF_)                                                        \
-  if (c.warps == W && c.cq == CQ_ && c.nstage == NS && c.ref_smem == RS && c.pf == PF_) \
-    return launch_stream_t<LAYOUT, MODE, CQ_, NS, RS, W, PF_>(a, smem, grid, st);
-  GB_CFG(16, 128, 2, true, 0)
-  GB_CFG(16, 64, 2, true, 8)
-  GB_CFG(16, 64, 2, true, 0)
-  GB_CFG(16, 64, 3, true, 4)
-  GB_CFG(16, 128, 2, true, 4)
-  GB_CFG(16, 64, 4, false, 4)
-  GB_CFG(8, 64, 4, true, 8)
-  GB_CFG(16, 64, 2, true, 16)
-  GB_CFG(8, 128, 4, false, 0)
+int launch_stream_m(const StreamArgs& a, const CUtensorMap& tm, const StreamCfg& c, size_t smem, int grid,
+                    cudaStream_t st) {
+#define GB_CFG(W, CQ_, NS, RS)                                                  \
+  if (c.warps == W && c.cq == CQ_ && c.nstage == NS && c.ref_smem == RS)       \
+    return launch_stream_t<LAYOUT, MODE, CQ_, NS, RS, W>(a, tm, smem, grid, st);
+  GB_CFG(16, 128, 2, true)
+  GB_CFG(16, 64, 3, true)
+  GB_CFG(16, 64, 2, true)
+  GB_CFG(16, 64, 4, false)
+  GB_CFG(8, 128, 3, true)
+  GB_CFG(8, 64, 4, true)
+  GB_CFG(8, 128, 4, false)
 #undef GB_CFG
   return set_error(GBRMSD_E_INVALID, "no streaming kernel for this configuration");
 }
 
 template <int LAYOUT>
-int launch_stream_l(int mode, const StreamArgs& a, const StreamCfg& c, size_t smem, int grid, cudaStream_t st) {
+int launch_stream_l(int mode, const StreamArgs& a, const CUtensorMap& tm, const StreamCfg& c, size_t smem,
+                    int grid, cudaStream_t st) {
   switch (mode) {
-    case MODE_CENTER: return launch_stream_m<LAYOUT, MODE_CENTER>(a, c, smem, grid, st);
-    case MODE_PRECENTERED: return launch_stream_m<LAYOUT, MODE_PRECENTERED>(a, c, smem, grid, st);
-    case MODE_NOSUPERPOSE: return launch_stream_m<LAYOUT, MODE_NOSUPERPOSE>(a, c, smem, grid, st);
-    default: return launch_stream_m<LAYOUT, MODE_TRACE>(a, c, smem, grid, st);
+    case MODE_CENTER: return launch_stream_m<LAYOUT, MODE_CENTER>(a, tm, c, smem, grid, st);
+    case MODE_PRECENTERED: return launch_stream_m<LAYOUT, MODE_PRECENTERED>(a, tm, c, smem, grid, st);
+    case MODE_NOSUPERPOSE: return launch_stream_m<LAYOUT, MODE_NOSUPERPOSE>(a, tm, c, smem, grid, st);
+    default: return launch_stream_m<LAYOUT, MODE_TRACE>(a, tm, c, smem, grid, st);
   }
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against libcuda).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+int encode_axis_map(CUtensorMap* tm, const StreamArgs& a) {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    GB_CUDA_TRY(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q),
+                "cudaGetDriverEntryPointByVersion(cuTensorMapEncodeTiled)");
+    if (q != cudaDriverEntryPointSuccess || !p)
+      return set_error(GBRMSD_E_UNSUPPORTED, "cuTensorMapEncodeTiled is not available");
+    fn = reinterpret_cast<EncodeTiledFn>(p);
+  }
+  // (atoms, axes, frames); box = 256 atoms x 3 axes x 1 frame
+  const cuuint64_t dims[3] = {(cuuint64_t)a.n_padded, 3, (cuuint64_t)a.n_frames};
+  const cuuint64_t strides[2] = {(cuuint64_t)a.n_padded * 4, (cuuint64_t)a.frame_stride * 4};
+  const cuuint32_t box[3] = {4 * BOX_QUADS, 3, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  const CUresult r = fn(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(a.x), dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return set_error(GBRMSD_E_INVALID, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return GBRMSD_OK;
 }
 
 int launch_stream(int layout, int mode, const StreamArgs& a, const StreamCfg& c, cudaStream_t st) {
   const bool use_ref = mode != MODE_TRACE;
   const size_t smem = stream_smem_bytes(c, a.n_padded, use_ref);
   const int grid = sm_count();
-  return layout == ATOM_MAJOR ? launch_stream_l<ATOM_MAJOR>(mode, a, c, smem, grid, st)
-                              : launch_stream_l<AXIS_MAJOR>(mode, a, c, smem, grid, st);
+  alignas(64) CUtensorMap tm;
+  memset(&tm, 0, sizeof(tm));
+  if (layout == AXIS_MAJOR) {
+    const int rc = encode_axis_map(&tm, a);
+    if (rc) return rc;
+    return launch_stream_l<AXIS_MAJOR>(mode, a, tm, c, smem, grid, st);
+  }
+  return launch_stream_l<ATOM_MAJOR>(mode, a, tm, c, smem, grid, st);
 }
 
 struct WsLayout {
@@ -1211,7 +1222,7 @@ int gbrmsd_stream_config_describe(int32_t index, int32_t n_atoms, int32_t* out5)
   out4[1] = c.cq;
   out4[2] = c.nstage;
   out4[3] = c.ref_smem ? 1 : 0;
-  out4[4] = c.pf;
+  out4[4] = 0;
   return cfg_fits(c, (n_atoms + 3) / 4 * 4, true) ? 1 : 0;
 }
 
