@@ -206,6 +206,9 @@ def rmsd_host_frames(x: np.ndarray, ref: "DeviceReference", mode: int, *, g_targ
     """
     device = require_device()
     F, A = x.shape[0], x.shape[1]
+    if F == 0 or A == 0:
+        # no atoms: the reference returns 0 for every frame (0/0 clamped)
+        return np.zeros(F, dtype=np.float32)
     Ap = padded(A)
     frame_bytes = 12 * max(A, 1)
     C = max(1, min(F, chunk_bytes // frame_bytes))
