@@ -95,6 +95,25 @@ int gbrmsd_rmsd_to_reference(const float* x, int64_t n_frames, int32_t n_atoms, 
                              int64_t self_index, float* out_rmsd, float* out_centroid,
                              float* out_trace, void* ws, size_t ws_bytes, void* stream);
 
+/* Allocation-free variant of gbrmsd_rmsd_to_reference.  It has no
+ * counterpart in the reference (mdtraj's CPU path never allocates device
+ * memory).  For callers that cannot allocate device memory at the point they
+ * need RMSDs -- code running during CUDA-graph capture, inside another
+ * runtime's memory pool, or a plugin without an allocator -- the scratch is a
+ * fixed 16 MiB device array inside the library (held by every GPU that loads
+ * the library until the process exits), so the call takes no workspace and
+ * calls no allocator.  Limit: 65,536 frames per call (any atom count); larger
+ * requests fail with GBRMSD_E_WORKSPACE before any work is queued.  The first
+ * call on a device resolves the array's address with that device current and
+ * should come before any stream capture.  Calls share the array: work of two
+ * calls that overlaps on the GPU races, so serialise them.  Arguments as for
+ * gbrmsd_rmsd_to_reference. */
+int gbrmsd_rmsd_to_reference_noalloc(const float* x, int64_t n_frames, int32_t n_atoms, int32_t n_padded,
+                                     int64_t frame_stride, int32_t layout, int32_t mode,
+                                     const void* ref_ws, const float* g_target, float g_ref,
+                                     int64_t self_index, float* out_rmsd, float* out_centroid,
+                                     float* out_trace, void* stream);
+
 /* ---- In-place centring ------------------------------------------------------
  * Replaces inplace_center_and_trace_atom_major (mdtraj/rmsd/include/center.h:7-8;
  * src/center_generic.h:3-44) for whole trajectories on the device, i.e. the

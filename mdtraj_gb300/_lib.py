@@ -45,6 +45,10 @@ SIGNATURES: dict[str, tuple] = {
         C.c_int,
         [_vp, _i64, _i32, _i32, _i64, _i32, _i32, _vp, _vp, _f32, _i64, _vp, _vp, _vp, _vp, _sz, _vp],
     ),
+    "gbrmsd_rmsd_to_reference_noalloc": (
+        C.c_int,
+        [_vp, _i64, _i32, _i32, _i64, _i32, _i32, _vp, _vp, _f32, _i64, _vp, _vp, _vp, _vp],
+    ),
     "gbrmsd_center_inplace": (C.c_int, [_vp, _i64, _i32, _i32, _i64, _i32, _vp, _vp, _vp, _sz, _vp]),
     "gbrmsd_workspace_status": (C.c_int, [_vp, _vp]),
     "gbrmsd_stream_config_count": (C.c_int, []),

@@ -1012,6 +1012,14 @@ static void prof_end(cudaStream_t st) {
 
 }  // namespace gb
 
+// Scratch of gbrmsd_rmsd_to_reference_noalloc: a fixed device array that
+// exists on every GPU that loads this library, for the life of the process.
+// 16 MiB covers the partial-sum records, refinement list and centroids of up
+// to 65,536 frames of any atom count on a 152-SM GB300.
+constexpr size_t kNoallocScratchBytes = 16u << 20;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
+static void* g_noalloc_scratch_addr[64] = {};
+
 using namespace gb;
 
 extern "C" {
@@ -1144,6 +1152,43 @@ int gbrmsd_rmsd_to_reference(const float* x, int64_t n_frames, int32_t n_atoms, 
     GB_CUDA_TRY(cudaGetLastError(), "launch refine_kernel");
   }
   return GBRMSD_OK;
+}
+
+// For callers that cannot allocate device memory when they need RMSDs -- for
+// example code that runs while a CUDA graph is being captured, inside another
+// runtime's memory pool, or in a plugin that has no allocator of its own --
+// this variant of gbrmsd_rmsd_to_reference takes no workspace: its scratch is
+// g_noalloc_scratch above.  It calls no cudaMalloc/cudaFree.  The first call
+// on a device looks up the array's device address (cudaGetSymbolAddress) with
+// that device current; make that first call before any stream capture.  All
+// calls share the one array and it keeps the last call's contents (the
+// per-call header is cleared on the stream before use), so calls whose work
+// overlaps on the GPU -- concurrent streams or threads -- race; serialise them.
+int gbrmsd_rmsd_to_reference_noalloc(const float* x, int64_t n_frames, int32_t n_atoms, int32_t n_padded,
+                                     int64_t frame_stride, int32_t layout, int32_t mode, const void* ref_ws,
+                                     const float* g_target, float g_ref, int64_t self_index, float* out_rmsd,
+                                     float* out_centroid, float* out_trace, void* stream) {
+  clear_error();
+  int dev = 0;
+  GB_CUDA_TRY(cudaGetDevice(&dev), "cudaGetDevice");
+  if (dev < 0 || dev >= 64) return set_error(GBRMSD_E_UNSUPPORTED, "rmsd_to_reference_noalloc: device %d", dev);
+  if (!g_noalloc_scratch_addr[dev]) {
+    void* p = nullptr;
+    GB_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress(g_noalloc_scratch)");
+    if (!p) return set_error(GBRMSD_E_CUDA, "rmsd_to_reference_noalloc: null scratch address");
+    g_noalloc_scratch_addr[dev] = p;
+  }
+  if (n_frames < 0 || n_atoms < 0) return set_error(GBRMSD_E_INVALID, "negative n_frames/n_atoms");
+  const size_t need = gbrmsd_rmsd_workspace_bytes(n_frames, n_atoms);
+  if (need > kNoallocScratchBytes)
+    return set_error(GBRMSD_E_WORKSPACE,
+                     "rmsd_to_reference_noalloc: %lld frames of %d atoms need %zu bytes of scratch but the static "
+                     "scratch holds %zu (at most 65536 frames per call); split the call or use "
+                     "gbrmsd_rmsd_to_reference with a workspace",
+                     (long long)n_frames, n_atoms, need, kNoallocScratchBytes);
+  return gbrmsd_rmsd_to_reference(x, n_frames, n_atoms, n_padded, frame_stride, layout, mode, ref_ws, g_target,
+                                  g_ref, self_index, out_rmsd, out_centroid, out_trace, g_noalloc_scratch_addr[dev],
+                                  kNoallocScratchBytes, stream);
 }
 
 int gbrmsd_center_inplace(float* x, int64_t n_frames, int32_t n_atoms, int32_t n_padded, int64_t frame_stride,
