@@ -114,6 +114,22 @@ int gbrmsd_rmsd_to_reference_noalloc(const float* x, int64_t n_frames, int32_t n
                                      int64_t self_index, float* out_rmsd, float* out_centroid,
                                      float* out_trace, void* stream);
 
+/* ---- All-pairs RMSD matrix --------------------------------------------------
+ * Replaces the clustering loop over md.rmsd(traj, traj, i, precentered=True)
+ * (mdtraj examples/clustering.ipynb, cell 6; _rmsd.pyx:64-243 per row): out is
+ * the symmetric n_frames x n_frames float32 matrix (row-major, diagonal 0).
+ * centre = 1 centres every frame first (float centroid, as
+ * Trajectory.center_coordinates); 0 uses the coordinates as given.
+ * method 0: FP32 CUDA-core tiles; method 1: split-BF16 (hi + lo) tcgen05
+ * tensor-core tiles with FP32 accumulation.  Both solve QCP per pair in FP32;
+ * near-identical pairs are recomputed exactly (compensated inner products,
+ * FP64 QCP, direct residual).  ws: gbrmsd_allpairs_workspace_bytes(...).
+ */
+size_t gbrmsd_allpairs_workspace_bytes(int64_t n_frames, int32_t n_atoms);
+int gbrmsd_allpairs(const float* x, int64_t n_frames, int32_t n_atoms, int32_t n_padded, int64_t frame_stride,
+                    int32_t layout, int32_t centre, int32_t method, float* out, void* ws, size_t ws_bytes,
+                    void* stream);
+
 /* ---- In-place centring ------------------------------------------------------
  * Replaces inplace_center_and_trace_atom_major (mdtraj/rmsd/include/center.h:7-8;
  * src/center_generic.h:3-44) for whole trajectories on the device, i.e. the

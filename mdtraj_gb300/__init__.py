@@ -13,7 +13,8 @@ buffers and streams.  There is no CPU fallback.
 from . import _lib  # loads libgbrmsd.so (raises ImportError if it was not built)
 from . import _rmsd
 from ._rmsd import rmsd
+from .allpairs import allpairs_rmsd
 from .trajectory import Trajectory
 
-__all__ = ["rmsd", "Trajectory", "_rmsd"]
+__all__ = ["rmsd", "allpairs_rmsd", "Trajectory", "_rmsd"]
 __version__ = "0.1.0"

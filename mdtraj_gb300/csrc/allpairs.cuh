@@ -1,0 +1,98 @@
+// All-pairs RMSD matrix: shared declarations.
+//
+// Work = the reference's clustering loop `for i: D[i] = md.rmsd(traj, traj,
+// i, precentered=True)` (mdtraj examples/clustering.ipynb, cell 6) done as
+// one symmetric matrix: frames are centred once (Trajectory.center_coordinates,
+// mdtraj/core/trajectory.py:2114-2137), stacked as X (3F x A) with row 3i+c =
+// axis c of frame i, and P = X X^T; the 3x3 block (i, j) of P is the inner
+// product matrix M_ij of msd_atom_major (mdtraj/rmsd/src/theobald_rmsd_generic.h:63-119),
+// fed to QCP per pair.
+#pragma once
+
+#include <stdint.h>
+
+#include "common.cuh"
+
+namespace gb {
+
+// Refinement record for a pair whose msd is too small for the per-pair FP32
+// QCP to resolve.
+struct PairRefine {
+  int32_t i, j;
+};
+
+struct AllPairsDims {
+  int64_t n_frames;
+  int32_t n_atoms;
+  int32_t k_pad;   // atoms padded to a multiple of 64 (BF16 K blocks)
+  int64_t rows;    // 3 * n_frames
+};
+
+constexpr int DEV_ERR_REFINE_OVERFLOW = 4;
+
+// FP32 QCP on the quartic normalised by lam0 = (Ga + Gb) / 2 (root near 1).
+// Returns msd = 2 lam0 (1 - x) / n; *x_out = normalised lambda_max.
+__device__ __forceinline__ float qcp_msd_f32(const float (&m)[9], float ga, float gb, float inv_n) {
+  const float lam0 = 0.5f * (ga + gb);
+  if (!(lam0 > 0.f)) return 0.f;
+  const float inv = 1.0f / lam0;
+  float mm[9];
+#pragma unroll
+  for (int t = 0; t < 9; ++t) mm[t] = m[t] * inv;
+  const float k00 = mm[0] + mm[4] + mm[8], k01 = mm[5] - mm[7], k02 = mm[6] - mm[2], k03 = mm[1] - mm[3];
+  const float k11 = mm[0] - mm[4] - mm[8], k12 = mm[1] + mm[3], k13 = mm[6] + mm[2];
+  const float k22 = -mm[0] + mm[4] - mm[8], k23 = mm[5] + mm[7], k33 = -mm[0] - mm[4] + mm[8];
+  float c2 = 0.f;
+#pragma unroll
+  for (int t = 0; t < 9; ++t) c2 = fmaf(mm[t], mm[t], c2);
+  c2 *= -2.f;
+  const float detm = mm[0] * (mm[4] * mm[8] - mm[5] * mm[7]) - mm[1] * (mm[3] * mm[8] - mm[5] * mm[6]) +
+                     mm[2] * (mm[3] * mm[7] - mm[4] * mm[6]);
+  const float c1 = -8.f * detm;
+  const float s01 = k00 * k11 - k01 * k01, s02 = k00 * k12 - k02 * k01, s03 = k00 * k13 - k03 * k01;
+  const float s12 = k01 * k12 - k02 * k11, s13 = k01 * k13 - k03 * k11, s23 = k02 * k13 - k03 * k12;
+  const float q01 = k02 * k13 - k12 * k03, q02 = k02 * k23 - k22 * k03, q03 = k02 * k33 - k23 * k03;
+  const float q12 = k12 * k23 - k22 * k13, q13 = k12 * k33 - k23 * k13, q23 = k22 * k33 - k23 * k23;
+  const float c0 = s01 * q23 - s02 * q13 + s03 * q12 + s12 * q03 - s13 * q02 + s23 * q01;
+  float x = 1.0f;
+#pragma unroll 1
+  for (int it = 0; it < 30; ++it) {
+    const float x2 = x * x;
+    const float b = (x2 + c2) * x;
+    const float a = b + c1;
+    const float pv = a * x + c0;
+    const float dp = 2.0f * x2 * x + b + a;
+    if (!(dp != 0.0f)) break;
+    const float step = __fdividef(pv, dp);
+    x -= step;
+    if (!(fabsf(step) > 2e-7f)) break;
+  }
+  const float msd = 2.0f * lam0 * (1.0f - x) * inv_n;
+  return msd > 0.f ? msd : 0.f;
+}
+
+// Writes the pair's rmsd to both triangles (i < j) or 0 on the diagonal and
+// queues near-identical pairs for refinement.
+__device__ __forceinline__ void pair_epilogue(int64_t i, int64_t j, const float (&m)[9], const double* __restrict__ G,
+                                              float inv_n, int64_t F, float* __restrict__ out, PairRefine* rl,
+                                              int* rc, int rcap, int* err) {
+  if (i == j) {
+    out[i * F + i] = 0.f;
+    return;
+  }
+  const float ga = (float)G[i], gb = (float)G[j];
+  const float msd = qcp_msd_f32(m, ga, gb, inv_n);
+  const float r = sqrtf(msd);
+  out[i * F + j] = r;
+  out[j * F + i] = r;
+  const float scale = 0.5f * (ga + gb) * inv_n;
+  if (r < 0.02f * scale) {
+    const int slot = atomicAdd(rc, 1);
+    if (slot < rcap)
+      rl[slot] = PairRefine{(int32_t)i, (int32_t)j};
+    else
+      atomicOr(err, DEV_ERR_REFINE_OVERFLOW);
+  }
+}
+
+}  // namespace gb

@@ -1,0 +1,417 @@
+// All-pairs RMSD on the 5th-generation tensor cores (tcgen05, sm_103a).
+//
+// P = X X^T with X = hi + lo split into two BF16 planes, computed as
+// hi.hi^T + hi.lo^T + lo.hi^T with FP32 accumulation in tensor memory
+// (the lo.lo^T term is ~2^-18 relative and dropped).  One tile is a
+// 128 x 240 block of P: 42 frames (126 rows + 2 ignored) by 80 frames.
+//
+// Persistent CTAs (one per SM), 192 threads:
+//   warp 0       TMA producer: per 64-atom k block, four 2-D tensor copies
+//                (A_hi, A_lo 128 x 64; B_hi, B_lo 240 x 64; 128-byte swizzle)
+//                into a 2-stage shared-memory ring;
+//   warp 1       allocates 512 TMEM columns (two 240-column accumulators),
+//                one lane issues 12 tcgen05.mma per k block (3 products x 4
+//                k-steps of 16), commits stage releases and accumulator-full
+//                to mbarriers;
+//   warps 2..5   epilogue: tcgen05.ld 48-column chunks (16 frames) into
+//                registers, stage them in shared memory, FP32 QCP per pair
+//                (allpairs.cuh), write both triangles; release the
+//                accumulator so the next tile's MMAs overlap this epilogue.
+// Every wait is bounded; on a timeout the thread records an error and leaves
+// its loop, and the CTA frees its tensor memory before exiting.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <string.h>
+
+#include <vector>
+
+#include "allpairs.cuh"
+#include "capi_internal.h"
+#include "common.cuh"
+
+namespace gb {
+namespace {
+
+constexpr int TILE_M = 128;             // rows of P per tile (tensor-core M)
+constexpr int TILE_N = 240;             // columns of P per tile (tensor-core N)
+constexpr int FR_M = 42;                // frames per tile row block (126 rows)
+constexpr int FR_N = 80;                // frames per tile column block
+constexpr int KBLK = 64;                // atoms per k block (128 B of BF16 = one swizzle row)
+constexpr int NSTAGE = 2;
+constexpr int A_BYTES = TILE_M * KBLK * 2;  // 16 KB
+constexpr int B_BYTES = TILE_N * KBLK * 2;  // 30 KB
+constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
+constexpr int EPI_COLS = 48;            // 16 frames per epilogue chunk
+constexpr int EPI_LD = EPI_COLS + 1;
+constexpr int EPI_BYTES = TILE_M * EPI_LD * 4;
+constexpr int TMEM_COLS = 512;
+constexpr int ACC_STRIDE = 256;         // TMEM columns between the two accumulators
+constexpr int NTHREADS = 192;
+constexpr uint32_t SPIN = 1u << 24;
+
+// smem: [stages | epilogue staging | barriers | tmem address]
+constexpr int SMEM_STAGES = NSTAGE * STAGE_BYTES;
+constexpr int SMEM_EPI = SMEM_STAGES;
+constexpr int SMEM_BAR = SMEM_EPI + ((EPI_BYTES + 127) / 128) * 128;
+constexpr int SMEM_TOTAL = SMEM_BAR + 128 + 1024;  // + slack for 1024-byte alignment
+
+struct TcArgs {
+  const double* G;
+  const int2* tiles;  // (row block, column block)
+  int64_t n_tiles;
+  int64_t F;
+  int32_t A;
+  int32_t kpad;
+  float* out;
+  PairRefine* rl;
+  int* rc;
+  int rcap;
+  int* err;
+};
+
+// ---- PTX wrappers ----------------------------------------------------------
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int32_t x, int32_t y, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
+          "r"(smem_addr(dst)),
+      "l"(map), "r"(x), "r"(y), "r"(smem_addr(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
+__device__ __forceinline__ void tc_alloc(uint32_t* dst_smem, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(dst_smem)),
+               "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void tc_relinquish() {
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tc_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc)
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_addr(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+#pragma unroll
+  for (int t = 0; t < 16; ++t) v[t] = __uint_as_float(r[t]);
+}
+__device__ __forceinline__ void tc_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+__device__ __forceinline__ void named_bar(int id, int n) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
+
+// Shared-memory matrix descriptor: K-major operand, 128-byte swizzle, rows of
+// 128 bytes, 8-row core groups 1024 bytes apart.
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFF) >> 4);  // start address
+  d |= (uint64_t)1 << 16;                  // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;        // stride byte offset
+  d |= (uint64_t)1 << 46;                  // descriptor version for tcgen05
+  d |= (uint64_t)2 << 61;                  // swizzle: 128 B
+  return d;
+}
+
+// Instruction descriptor: kind::f16, BF16 x BF16 -> F32, both K-major, M x N.
+__host__ __device__ constexpr uint32_t make_idesc(int m, int n) {
+  return (1u << 4)                       // D format F32
+         | (1u << 7)                     // A format BF16
+         | (1u << 10)                    // B format BF16
+         | ((uint32_t)(n >> 3) << 17)    // N / 8
+         | ((uint32_t)(m >> 4) << 24);   // M / 16
+}
+
+__device__ __forceinline__ bool wait_bar(uint64_t* bar, uint32_t parity, int* err) {
+  return mbar_wait_bounded(bar, parity, err, SPIN);
+}
+
+__global__ void __launch_bounds__(NTHREADS, 1) allpairs_tc_kernel(const __grid_constant__ CUtensorMap map_hi_a,
+                                                                  const __grid_constant__ CUtensorMap map_lo_a,
+                                                                  const __grid_constant__ CUtensorMap map_hi_b,
+                                                                  const __grid_constant__ CUtensorMap map_lo_b,
+                                                                  const TcArgs args) {
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* smem =
+      reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  float* sD = reinterpret_cast<float*>(smem + SMEM_EPI);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + SMEM_BAR);
+  uint64_t* full = bars;                 // [NSTAGE]
+  uint64_t* empty = bars + NSTAGE;       // [NSTAGE]
+  uint64_t* accfull = bars + 2 * NSTAGE; // [2]
+  uint64_t* accempty = accfull + 2;      // [2]
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accempty + 2);
+
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NSTAGE; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&accfull[b], 1);
+      mbar_init(&accempty[b], 4);
+    }
+    fence_mbar_init();
+  }
+  if (warp == 1) {
+    tc_alloc(tmem_slot, TMEM_COLS);
+    tc_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_base = *tmem_slot;
+
+  const int64_t n_tiles = args.n_tiles;
+  const int nkb = args.kpad / KBLK;
+  const int64_t rows_total = 3 * args.F;
+  (void)rows_total;
+
+  if (warp == 0) {
+    // ---------------- TMA producer ----------------
+    if (lane == 0) {
+      uint32_t it = 0;
+      bool ok = true;
+      for (int64_t t = blockIdx.x; t < n_tiles && ok; t += gridDim.x) {
+        const int2 tl = args.tiles[t];
+        const int32_t row_a = tl.x * (3 * FR_M), row_b = tl.y * (3 * FR_N);
+        for (int kb = 0; kb < nkb; ++kb, ++it) {
+          const int s = it % NSTAGE;
+          const uint32_t use = it / NSTAGE;
+          if (use > 0 && !wait_bar(&empty[s], (use - 1) & 1, args.err)) { ok = false; break; }
+          unsigned char* st = smem + s * STAGE_BYTES;
+          mbar_arrive_expect_tx(&full[s], STAGE_BYTES);
+          tma_load_2d(st, &map_hi_a, kb * KBLK, row_a, &full[s]);
+          tma_load_2d(st + A_BYTES, &map_lo_a, kb * KBLK, row_a, &full[s]);
+          tma_load_2d(st + 2 * A_BYTES, &map_hi_b, kb * KBLK, row_b, &full[s]);
+          tma_load_2d(st + 2 * A_BYTES + B_BYTES, &map_lo_b, kb * KBLK, row_b, &full[s]);
+        }
+      }
+      // drain: the last use of every stage must be consumed before the CTA exits
+      for (uint32_t k = (it > NSTAGE ? it - NSTAGE : 0); k < it; ++k) {
+        const int s = k % NSTAGE;
+        if (!wait_bar(&empty[s], (k / NSTAGE) & 1, args.err)) break;
+      }
+    }
+  } else if (warp == 1) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      constexpr uint32_t idesc = make_idesc(TILE_M, TILE_N);
+      uint32_t it = 0, tcount = 0;
+      bool ok = true;
+      for (int64_t t = blockIdx.x; t < n_tiles && ok; t += gridDim.x, ++tcount) {
+        const int b = tcount & 1;
+        const uint32_t buse = tcount >> 1;
+        if (buse > 0 && !wait_bar(&accempty[b], (buse - 1) & 1, args.err)) { ok = false; break; }
+        tc_fence_after();
+        const uint32_t d_tmem = tmem_base + b * ACC_STRIDE;
+        for (int kb = 0; kb < nkb; ++kb, ++it) {
+          const int s = it % NSTAGE;
+          if (!wait_bar(&full[s], (it / NSTAGE) & 1, args.err)) { ok = false; break; }
+          tc_fence_after();
+          const uint32_t st = smem_addr(smem + s * STAGE_BYTES);
+          const uint32_t a_hi = st, a_lo = st + A_BYTES, b_hi = st + 2 * A_BYTES, b_lo = st + 2 * A_BYTES + B_BYTES;
+#pragma unroll
+          for (int ks = 0; ks < KBLK / 16; ++ks) {
+            const uint32_t koff = ks * 32;  // 16 BF16 = 32 bytes inside the 128-byte swizzle row
+            const uint32_t acc0 = (kb > 0 || ks > 0) ? 1u : 0u;
+            tc_mma(d_tmem, smem_desc_sw128(a_hi + koff), smem_desc_sw128(b_hi + koff), idesc, acc0);
+            tc_mma(d_tmem, smem_desc_sw128(a_hi + koff), smem_desc_sw128(b_lo + koff), idesc, 1u);
+            tc_mma(d_tmem, smem_desc_sw128(a_lo + koff), smem_desc_sw128(b_hi + koff), idesc, 1u);
+          }
+          tc_commit(&empty[s]);  // stage reusable once these MMAs have read it
+        }
+        if (!ok) break;
+        tc_commit(&accfull[b]);  // accumulator complete
+      }
+      // wait for the last commits so no MMA is in flight when TMEM is freed
+      if (tcount > 0) {
+        const uint32_t lt = tcount - 1;
+        wait_bar(&accfull[lt & 1], (lt >> 1) & 1, args.err);
+      }
+    }
+  } else {
+    // ---------------- epilogue (warps 2..5) ----------------
+    const int ew = warp - 2;                 // 0..3
+    const int slice = warp & 3;              // TMEM lanes [32*slice, 32*slice + 32)
+    const int row = slice * 32 + lane;       // accumulator row of this thread
+    const int etid = ew * 32 + lane;         // 0..127
+    const float inv_n = 1.0f / (float)args.A;
+    volatile int* go = reinterpret_cast<volatile int*>(tmem_slot + 1);
+    uint32_t tcount = 0;
+    for (int64_t t = blockIdx.x; t < n_tiles; t += gridDim.x, ++tcount) {
+      const int b = tcount & 1;
+      const uint32_t buse = tcount >> 1;
+      // one thread waits; the four epilogue warps then agree on the outcome
+      if (etid == 0) *go = wait_bar(&accfull[b], buse & 1, args.err) ? 1 : 0;
+      named_bar(1, 128);
+      const int proceed = *go;
+      named_bar(1, 128);
+      if (!proceed) break;
+      tc_fence_after();
+      const int2 tl = args.tiles[t];
+      const int64_t i0 = (int64_t)tl.x * FR_M, j0 = (int64_t)tl.y * FR_N;
+      for (int ch = 0; ch < TILE_N / EPI_COLS; ++ch) {
+        const uint32_t taddr =
+            tmem_base + (uint32_t)(b * ACC_STRIDE + ch * EPI_COLS) + ((uint32_t)(slice * 32) << 16);
+        float v0[16], v1[16], v2[16];
+        tc_ld16(taddr, v0);
+        tc_ld16(taddr + 16, v1);
+        tc_ld16(taddr + 32, v2);
+        tc_wait_ld();
+        float* dst = sD + row * EPI_LD;
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+          dst[q] = v0[q];
+          dst[16 + q] = v1[q];
+          dst[32 + q] = v2[q];
+        }
+        named_bar(1, 128);
+        for (int p = etid; p < FR_M * 16; p += 128) {
+          const int li = p >> 4, lj = p & 15;
+          const int64_t i = i0 + li, j = j0 + ch * 16 + lj;
+          if (i < args.F && j < args.F && i <= j) {
+            float m[9];
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+#pragma unroll
+              for (int d = 0; d < 3; ++d) m[3 * c + d] = sD[(3 * li + c) * EPI_LD + 3 * lj + d];
+            pair_epilogue(i, j, m, args.G, inv_n, args.F, args.out, args.rl, args.rc, args.rcap, args.err);
+          }
+        }
+        named_bar(1, 128);
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&accempty[b]);
+    }
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    tc_dealloc(tmem_base, TMEM_COLS);
+  }
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+int encode_plane(CUtensorMap* tm, const void* base, int64_t rows, int32_t kpad, int box_rows) {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    GB_CUDA_TRY(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q),
+                "cudaGetDriverEntryPointByVersion(cuTensorMapEncodeTiled)");
+    if (q != cudaDriverEntryPointSuccess || !p) return set_error(GBRMSD_E_UNSUPPORTED, "cuTensorMapEncodeTiled missing");
+    fn = reinterpret_cast<EncodeTiledFn>(p);
+  }
+  const cuuint64_t dims[2] = {(cuuint64_t)kpad, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)kpad * 2};
+  const cuuint32_t box[2] = {KBLK, (cuuint32_t)box_rows};
+  const cuuint32_t estr[2] = {1, 1};
+  const CUresult r = fn(tm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return set_error(GBRMSD_E_INVALID, "cuTensorMapEncodeTiled (bf16 plane) failed: %d", (int)r);
+  return GBRMSD_OK;
+}
+
+// Tile list: groups of 8 row blocks, column-major inside a group, so tiles
+// that run concurrently share column blocks (and row blocks) in L2.
+std::vector<int2> make_tiles(int64_t F) {
+  const int64_t nbr = (F + FR_M - 1) / FR_M, nbc = (F + FR_N - 1) / FR_N;
+  std::vector<int2> tiles;
+  const int64_t grp = 8;
+  for (int64_t g0 = 0; g0 < nbr; g0 += grp) {
+    const int64_t g1 = g0 + grp < nbr ? g0 + grp : nbr;
+    for (int64_t cb = 0; cb < nbc; ++cb)
+      for (int64_t rb = g0; rb < g1; ++rb) {
+        // needed iff some pair (i, j) of the tile has i <= j
+        if (cb * FR_N + FR_N - 1 >= rb * FR_M) tiles.push_back(make_int2((int)rb, (int)cb));
+      }
+  }
+  return tiles;
+}
+
+}  // namespace
+
+int launch_allpairs_tc(const __nv_bfloat16* Xhi, const __nv_bfloat16* Xlo, const double* G, int64_t F, int32_t A,
+                       int32_t kpad, float* out, PairRefine* rl, int* rc, int rcap, int* err, cudaStream_t st) {
+  if (kpad % KBLK) return set_error(GBRMSD_E_INVALID, "allpairs_tc: k padding must be a multiple of 64");
+  if (max_dyn_smem() < SMEM_TOTAL) return set_error(GBRMSD_E_UNSUPPORTED, "allpairs_tc: not enough shared memory");
+  const int64_t rows = 3 * F;
+  alignas(64) CUtensorMap mha, mla, mhb, mlb;
+  memset(&mha, 0, sizeof(mha));
+  memset(&mla, 0, sizeof(mla));
+  memset(&mhb, 0, sizeof(mhb));
+  memset(&mlb, 0, sizeof(mlb));
+  int rc0 = encode_plane(&mha, Xhi, rows, kpad, TILE_M);
+  if (!rc0) rc0 = encode_plane(&mla, Xlo, rows, kpad, TILE_M);
+  if (!rc0) rc0 = encode_plane(&mhb, Xhi, rows, kpad, TILE_N);
+  if (!rc0) rc0 = encode_plane(&mlb, Xlo, rows, kpad, TILE_N);
+  if (rc0) return rc0;
+  const std::vector<int2> tiles = make_tiles(F);
+  // tile list lives right after the refinement list in the caller's workspace
+  int2* dtiles = reinterpret_cast<int2*>(reinterpret_cast<unsigned char*>(rl) + align_up((size_t)rcap * sizeof(PairRefine), 256));
+  GB_CUDA_TRY(cudaMemcpyAsync(dtiles, tiles.data(), tiles.size() * sizeof(int2), cudaMemcpyHostToDevice, st),
+              "copy tile list");
+  TcArgs a;
+  a.G = G;
+  a.tiles = dtiles;
+  a.n_tiles = (int64_t)tiles.size();
+  a.F = F;
+  a.A = A;
+  a.kpad = kpad;
+  a.out = out;
+  a.rl = rl;
+  a.rc = rc;
+  a.rcap = rcap;
+  a.err = err;
+  GB_CUDA_TRY(cudaFuncSetAttribute(allpairs_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_TOTAL),
+              "cudaFuncSetAttribute(allpairs_tc_kernel)");
+  const int64_t grid = a.n_tiles < sm_count() ? a.n_tiles : sm_count();
+  allpairs_tc_kernel<<<(unsigned)grid, NTHREADS, SMEM_TOTAL, st>>>(mha, mla, mhb, mlb, a);
+  GB_CUDA_TRY(cudaGetLastError(), "launch allpairs_tc_kernel");
+  // (a pageable host->device cudaMemcpyAsync returns once the source has been
+  // staged, so the host tile list may go out of scope here)
+  return GBRMSD_OK;
+}
+
+size_t allpairs_tc_tiles_bytes(int64_t F) {
+  const int64_t nbr = (F + FR_M - 1) / FR_M, nbc = (F + FR_N - 1) / FR_N;
+  return align_up((size_t)(nbr * nbc) * sizeof(int2), 256);
+}
+
+}  // namespace gb

@@ -124,3 +124,55 @@ def device_single_reference(n_frames: int, n_atoms: int, n_padded: int, layout: 
             out[s:e, :, :n_atoms] = fr.transpose(1, 2)
         del fr, noise
     return ref.to(torch.float32), out, sig
+
+
+def metastable_walk(n_frames: int, n_atoms: int, n_centres: int = 50, seed: int = 0, sigma: float = 0.1,
+                    cube: float = 5.0, stay: float = 0.99):
+    """All-pairs workload: a seeded Markov random walk over `n_centres`
+    metastable structures (atoms uniform in a `cube` nm cube); frame =
+    R (centre + N(0, sigma^2)), R Haar-random.  Returns (labels, frames)
+    with frames float32 (F, A, 3)."""
+    rng = np.random.default_rng(seed)
+    centres = rng.uniform(0.0, cube, size=(n_centres, n_atoms, 3))
+    labels = np.empty(n_frames, dtype=np.int64)
+    s = int(rng.integers(n_centres))
+    for f in range(n_frames):
+        if rng.random() > stay:
+            s = int(rng.integers(n_centres))
+        labels[f] = s
+    frames = np.empty((n_frames, n_atoms, 3), dtype=np.float32)
+    for s0 in range(0, n_frames, 1024):
+        e = min(n_frames, s0 + 1024)
+        rot = haar_rotations(e - s0, rng)
+        pts = centres[labels[s0:e]] + rng.normal(size=(e - s0, n_atoms, 3)) * sigma
+        frames[s0:e] = np.einsum("fkj,fij->fki", pts, rot)
+    return labels, frames
+
+
+def device_metastable_walk(n_frames: int, n_atoms: int, n_padded: int, seed: int, device, n_centres: int = 50,
+                           sigma: float = 0.1, cube: float = 5.0, stay: float = 0.99, chunk: int = 1024):
+    """Device version of metastable_walk into a padded atom-major buffer
+    (F, n_padded * 3); padding atoms are zero."""
+    import torch
+
+    rng = np.random.default_rng(seed)
+    g = torch.Generator(device=device)
+    g.manual_seed(int(seed))
+    centres = torch.rand((n_centres, n_atoms, 3), generator=g, device=device, dtype=torch.float64) * cube
+    labels = np.empty(n_frames, dtype=np.int64)
+    s = int(rng.integers(n_centres))
+    for f in range(n_frames):
+        if rng.random() > stay:
+            s = int(rng.integers(n_centres))
+        labels[f] = s
+    lab = torch.from_numpy(labels).to(device)
+    out = torch.zeros((n_frames, n_padded * 3), dtype=torch.float32, device=device)
+    for s0 in range(0, n_frames, chunk):
+        e = min(n_frames, s0 + chunk)
+        q = torch.randn((e - s0, 4), generator=g, device=device, dtype=torch.float64)
+        rot = _torch_rot_from_quat(q)
+        pts = centres[lab[s0:e]] + torch.randn((e - s0, n_atoms, 3), generator=g, device=device,
+                                               dtype=torch.float64) * sigma
+        fr = torch.einsum("fkj,fij->fki", pts, rot).to(torch.float32)
+        out[s0:e].view(e - s0, n_padded, 3)[:, :n_atoms, :] = fr
+    return labels, out
