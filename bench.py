@@ -44,6 +44,8 @@ WORKLOADS = {
     # name: (n_frames, n_atoms, layout, sigma_lo, sigma_hi, exact_fraction)
     "single_reference_200000x10000": (200_000, 10_000, 1, 0.005, 0.5, 0.01),
     "single_reference_10000x1000": (10_000, 1_000, 0, 0.05, 0.05, 0.0),
+    # all-pairs matrix: (n_frames, n_atoms, n_centres, sigma, cube, stay)
+    "allpairs_20000x2000": (20_000, 2_000, 50, 0.1, 5.0, 0.99),
 }
 DEFAULT_WORKLOAD = "single_reference_200000x10000"
 
@@ -172,15 +174,16 @@ def time_cpu_reference(n_atoms: int, budget_s: float, sigma_lo: float, sigma_hi:
     frames = 0
     t_total = 0.0
     reps = 0
+    # md.rmsd centres its inputs in place; repeating it on the same arrays
+    # repeats the same work (both centring passes and the msd pass), as a
+    # caller looping md.rmsd over a trajectory does.
     while t_total < budget_s or reps < 2:
-        xs = x.copy()
-        rs = ref.copy()
         t0 = time.perf_counter()
-        impl.md_rmsd(xs, rs)
+        impl.md_rmsd(x, ref)
         t_total += time.perf_counter() - t0
         frames += n_sample
         reps += 1
-        if reps >= 200:
+        if reps >= 100000:
             break
     return {"value": frames / t_total, "unit": "frames/s", "cores": cpu.n_threads(), "kind": impl.kind,
             "sample": f"{reps} x md.rmsd over {n_sample} frames x {n_atoms} atoms (same generator, "
@@ -373,11 +376,188 @@ def run_e2e(args, F, A, s_lo, s_hi, exact, dev) -> dict:
             "steps": args.e2e_steps}
 
 
+# ---------------------------------------------------------------------------
+# All-pairs matrix workload
+# ---------------------------------------------------------------------------
+
+
+def run_allpairs(args) -> dict:
+    """Symmetric RMSD matrix of 20,000 frames x 2,000 atoms (random walk over
+    50 metastable centres, sigma 0.1 nm, random rotations).  One step = the
+    full matrix with the split-BF16 tensor-core path; the plain FP32
+    CUDA-core path is timed on the same input for comparison."""
+    import torch
+
+    from mdtraj_gb300 import _device as D
+    from mdtraj_gb300 import _lib, synth
+    from mdtraj_gb300.allpairs import METHODS
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    F, A, C, sig, cube, stay = WORKLOADS[args.workload]
+    if args.frames:
+        F = args.frames
+    Ap = D.padded(A)
+    labels, x = synth.device_metastable_walk(F, A, Ap, seed=77 + rank, device=dev, n_centres=C, sigma=sig,
+                                             cube=cube, stay=stay)
+    lib = _lib.lib
+    ws = D.empty_bytes(lib.gbrmsd_allpairs_workspace_bytes(F, A), dev)
+    out = torch.empty((F, F), dtype=torch.float32, device=dev)
+    stream = D.stream_handle()
+
+    def step(method):
+        _lib.check(lib.gbrmsd_allpairs(x.data_ptr(), F, A, Ap, 3 * Ap, _lib.ATOM_MAJOR, 1, METHODS[method],
+                                       out.data_ptr(), ws.data_ptr(), ws.numel(), stream))
+
+    def timed(method, steps, warmup):
+        for _ in range(warmup):
+            step(method)
+        torch.cuda.synchronize()
+        lib.gbrmsd_profile_enable(steps)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            step(method)
+        e1.record()
+        torch.cuda.synchronize()
+        k = np.zeros(steps, dtype=np.float32)
+        n = lib.gbrmsd_profile_read(k.ctypes.data, steps)
+        lib.gbrmsd_profile_enable(0)
+        refined = np.zeros(1, dtype=np.int32)
+        _lib.check(lib.gbrmsd_allpairs_status(ws.data_ptr(), refined.ctypes.data, stream))
+        return e0.elapsed_time(e1) / steps, float(np.mean(k[:n])), int(refined[0])
+
+    with ClockSampler(local) as clk:
+        ms_step, k_ms, refined = timed("tensor", args.steps, args.warmup)
+    out_t = out.clone()
+    fp32_steps = max(1, min(2, args.steps))
+    ms_fp32, k_fp32, _ = timed("fp32", fp32_steps, 1)
+    pairs = F * (F - 1) / 2
+    value = world * pairs / (ms_step / 1e3)
+    peaks = measured_peaks()
+    p = ROOT / "MEASURED_PEAKS.json"
+    bf16_peak = json.loads(p.read_text())["bf16_tflops"] if p.exists() else 1900.0
+    alg_flops = 3 * 18.0 * A * pairs            # three BF16 products of 9 MACs per atom per pair
+    achieved = alg_flops / (k_ms / 1e3) / 1e12
+    roof = {"bound": "tensor", "achieved": round(achieved, 1), "peak": bf16_peak, "unit": "TFLOP/s",
+            "frac": round(achieved / bf16_peak, 4), "traffic": traffic_from_profiles("allpairs_tc_kernel", args.workload),
+            "kernel": "allpairs_tc_kernel", "kernel_ms": round(k_ms, 4),
+            "algorithmic_flops_per_launch": alg_flops, "peak_src": "measured" if p.exists() else "fallback"}
+    acc = allpairs_accuracy(x, out_t, F, A, Ap, rank)
+    cpu_base = None
+    if rank == 0 and world == 1 and not args.skip_cpu:
+        cpu_base = time_cpu_allpairs(A, args.cpu_budget, C, sig, cube)
+    e2e = None
+    if rank == 0 and not args.skip_e2e:
+        e2e = allpairs_e2e(x, F, A, Ap, args)
+    return {
+        "metric": "rmsd_pairs_per_s",
+        "value": round(value, 1),
+        "unit": "pairs/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms_step, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "bf16x3 (split hi/lo, f32 accumulate)",
+        "data": "synthetic (seeded, generated on device)",
+        "config": {"workload": args.workload, "n_frames": F, "n_atoms": A, "centres": C, "sigma_nm": sig,
+                   "output": "full symmetric %d x %d float32" % (F, F),
+                   "l2": "operands (%.2f GB BF16 hi+lo) and output (%.2f GB) larger than L2; no flush"
+                         % (3.0 * F * ((A + 63) // 64 * 64) * 2 * 2 / 1e9, 4.0 * F * F / 1e9)},
+        "roofline": roof,
+        "fp32_cuda_core": {"ms_per_step": round(ms_fp32, 3), "kernel_ms": round(k_fp32, 3),
+                           "pairs_per_s": round(pairs / (ms_fp32 / 1e3), 1),
+                           "tensor_speedup_kernel": round(k_fp32 / k_ms, 2),
+                           "tensor_speedup_step": round(ms_fp32 / ms_step, 2)},
+        "refined_pairs": refined,
+        "cpu_baseline": cpu_base,
+        "e2e": e2e,
+        "gpu_launches": 3 * args.steps,
+        "clocks": clk.summary(),
+        "accuracy": acc,
+    }
+
+
+def allpairs_accuracy(x, out, F, A, Ap, rank, n_pairs=100_000) -> dict:
+    from oracle import fp64
+
+    rng = np.random.default_rng(11 + rank)
+    i = rng.integers(0, F, n_pairs)
+    j = rng.integers(0, F, n_pairs)
+    keep = i != j
+    pairs = np.stack([i[keep], j[keep]], 1)
+    frames = x.view(F, Ap, 3)[:, :A].cpu().numpy()
+    want = fp64.kabsch_rmsd_pairs(frames, pairs)
+    got = out[pairs[:, 0], pairs[:, 1]].cpu().numpy().astype(np.float64)
+    err = np.abs(got - want)
+    return {"checked_pairs": int(len(pairs)), "max_err_nm": float(err.max()), "rms_err_nm": float(np.sqrt((err ** 2).mean())),
+            "oracle": "FP64 Kabsch/SVD (oracle/fp64.py)"}
+
+
+def time_cpu_allpairs(A, budget_s, C, sig, cube) -> dict:
+    """Reference CPU path of the clustering loop: precentered md.rmsd rows
+    (getMultipleRMSDs_atom_major of the reference kernels) over a sample of
+    rows of a 20,000-frame trajectory sample; pairs/s."""
+    from mdtraj_gb300 import synth
+    from oracle import cpu
+
+    impl = cpu.best_available()
+    n_frames = 4000
+    labels, x = synth.metastable_walk(n_frames, A, n_centres=C, seed=5, sigma=sig, cube=cube)
+    g = impl.center_inplace(x)
+    rows = 0
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < budget_s and rows < n_frames:
+        impl.multiple(x, x, g, g, rows, axis_major=False)
+        rows += 1
+    dt = time.perf_counter() - t0
+    return {"value": rows * n_frames / dt, "unit": "pairs/s", "cores": cpu.n_threads(), "kind": impl.kind,
+            "sample": f"{rows} rows x {n_frames} frames x {A} atoms of md.rmsd(traj, traj, i, precentered=True) "
+                      f"({dt:.1f} s, OpenMP threads={cpu.n_threads()})"}
+
+
+def allpairs_e2e(x, F, A, Ap, args) -> dict:
+    """mdtraj_gb300.allpairs_rmsd on a host numpy trajectory: host->device
+    coordinates, the matrix, device->host of the full F x F result."""
+    import torch
+
+    import mdtraj_gb300 as md
+
+    host = x.view(F, Ap, 3)[:, :A].contiguous().cpu().numpy()
+    md.allpairs_rmsd(host[:64], method="tensor")
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(args.e2e_steps):
+        t0 = time.perf_counter()
+        md.allpairs_rmsd(host, method="tensor")
+        times.append(time.perf_counter() - t0)
+    t = float(np.mean(times))
+    return {"value": round(F * (F - 1) / 2 / t, 1), "unit": "pairs/s", "h2d_bytes_per_step": int(F * A * 12),
+            "d2h_bytes_per_step": int(F * F * 4), "ms_per_step": round(t * 1e3, 2),
+            "api": "mdtraj_gb300.allpairs_rmsd(host float32 (F, A, 3), method='tensor')", "steps": args.e2e_steps}
+
+
 def run_reference(args) -> dict:
     rank, world, local = dist_env()
-    F, A, layout, s_lo, s_hi, exact = WORKLOADS[args.workload]
     if rank != 0:
         return None
+    if args.workload.startswith("allpairs"):
+        F, A, C, sig, cube, stay = WORKLOADS[args.workload]
+        base = time_cpu_allpairs(A, args.cpu_budget, C, sig, cube)
+        return {"impl": "reference", "metric": "rmsd_pairs_per_s", "value": round(base["value"], 1),
+                "unit": "pairs/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": round(F * (F - 1) / 2 / base["value"] * 1e3, 2), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+                "config": {"workload": args.workload, "n_frames": F, "n_atoms": A,
+                           "note": "each step timed on a bounded row sample"},
+                "cpu_baseline": base,
+                "e2e": {"value": round(base["value"], 1), "unit": "pairs/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+    F, A, layout, s_lo, s_hi, exact = WORKLOADS[args.workload]
     base = time_cpu_reference(A, args.cpu_budget, s_lo, s_hi)
     per_step_s = F / base["value"]
     return {
@@ -419,6 +599,8 @@ def main():
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         res = run_reference(args)
+    elif args.workload.startswith("allpairs"):
+        res = run_allpairs(args)
     else:
         res = run_gpu(args)
     rank = int(os.environ.get("RANK", "0"))

@@ -130,6 +130,10 @@ int gbrmsd_allpairs(const float* x, int64_t n_frames, int32_t n_atoms, int32_t n
                     int32_t layout, int32_t centre, int32_t method, float* out, void* ws, size_t ws_bytes,
                     void* stream);
 
+/* Synchronises `stream`; reports how many pairs the last gbrmsd_allpairs on
+ * this workspace refined exactly and whether a device error was recorded. */
+int gbrmsd_allpairs_status(const void* ws, int32_t* refined_pairs, void* stream);
+
 /* ---- In-place centring ------------------------------------------------------
  * Replaces inplace_center_and_trace_atom_major (mdtraj/rmsd/include/center.h:7-8;
  * src/center_generic.h:3-44) for whole trajectories on the device, i.e. the
@@ -157,9 +161,9 @@ int gbrmsd_stream_config_count(void);
 int gbrmsd_stream_config_select(int32_t index);
 int gbrmsd_stream_config_describe(int32_t index, int32_t n_atoms, int32_t* out5);
 
-/* Timing of the streaming kernel (the dominant kernel of
- * gbrmsd_rmsd_to_reference) with CUDA events recorded on the caller's stream,
- * for benchmarks.  gbrmsd_profile_enable(n) arms recording for the next n
+/* Timing of the dominant kernel of gbrmsd_rmsd_to_reference (streaming
+ * kernel) and gbrmsd_allpairs (tile kernel) with CUDA events recorded on the
+ * caller's stream, for benchmarks.  gbrmsd_profile_enable(n) arms recording for the next n
  * calls (0 disables; n <= 4096); gbrmsd_profile_read waits for the recorded
  * calls, writes up to `capacity` kernel times in milliseconds, re-arms, and
  * returns how many it wrote (negative on error).  Not thread-safe. */

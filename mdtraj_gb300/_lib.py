@@ -51,6 +51,7 @@ SIGNATURES: dict[str, tuple] = {
     ),
     "gbrmsd_allpairs_workspace_bytes": (_sz, [_i64, _i32]),
     "gbrmsd_allpairs": (C.c_int, [_vp, _i64, _i32, _i32, _i64, _i32, _i32, _i32, _vp, _vp, _sz, _vp]),
+    "gbrmsd_allpairs_status": (C.c_int, [_vp, _vp, _vp]),
     "gbrmsd_center_inplace": (C.c_int, [_vp, _i64, _i32, _i32, _i64, _i32, _vp, _vp, _vp, _sz, _vp]),
     "gbrmsd_workspace_status": (C.c_int, [_vp, _vp]),
     "gbrmsd_stream_config_count": (C.c_int, []),

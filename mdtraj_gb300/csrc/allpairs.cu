@@ -9,7 +9,7 @@
 //                         buffering): the yardstick for the tensor path.
 //   pair epilogue         FP32 QCP on the quartic normalised by its upper
 //                         bound; msd = 2 lam0 (1 - x) / n.  Pairs closer than
-//                         0.02 * scale (scale = (Ga + Gb) / 2n, nm^2 -> nm)
+//                         0.25 * scale / sqrt(n) (scale = (Ga + Gb) / 2n)
 //                         are queued for allpairs_refine_kernel.
 //   allpairs_refine_kernel warp per queued pair: compensated M, FP64 QCP,
 //                         then the direct residual |R a_i - a_j|^2.
@@ -322,6 +322,18 @@ size_t gbrmsd_allpairs_workspace_bytes(int64_t n_frames, int32_t n_atoms) {
   return ap_ws(n_frames, n_atoms).total;
 }
 
+int gbrmsd_allpairs_status(const void* ws, int32_t* refined_pairs, void* stream) {
+  clear_error();
+  if (!ws) return set_error(GBRMSD_E_INVALID, "allpairs_status: null workspace");
+  int h[2] = {0, 0};
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  GB_CUDA_TRY(cudaMemcpyAsync(h, ws, sizeof(h), cudaMemcpyDeviceToHost, st), "copy allpairs header");
+  GB_CUDA_TRY(cudaStreamSynchronize(st), "sync");
+  if (refined_pairs) *refined_pairs = h[1];
+  if (h[0]) return set_error(GBRMSD_E_DEVICE, "allpairs device error word 0x%x (1 = wait expired, 4 = refinement list full)", h[0]);
+  return GBRMSD_OK;
+}
+
 int gbrmsd_allpairs(const float* x, int64_t n_frames, int32_t n_atoms, int32_t n_padded, int64_t frame_stride,
                     int32_t layout, int32_t centre, int32_t method, float* out, void* ws, size_t ws_bytes,
                     void* stream) {
@@ -360,12 +372,16 @@ int gbrmsd_allpairs(const float* x, int64_t n_frames, int32_t n_atoms, int32_t n
     if (tiles > 0x7fffffffLL) return set_error(GBRMSD_E_INVALID, "allpairs: too many tiles");
     GB_CUDA_TRY(cudaFuncSetAttribute(allpairs_fp32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, FP32_TILE_SMEM),
                 "cudaFuncSetAttribute(allpairs_fp32_kernel)");
+    prof_begin(st);
     allpairs_fp32_kernel<<<(unsigned)tiles, 256, FP32_TILE_SMEM, st>>>(X32, G, n_frames, n_atoms, kpad, nb, out, rl,
                                                                        hdr + 1, L.rcap, hdr);
     GB_CUDA_TRY(cudaGetLastError(), "launch allpairs_fp32_kernel");
+    prof_end(st);
   } else {
+    prof_begin(st);
     const int rc = launch_allpairs_tc(Xhi, Xlo, G, n_frames, n_atoms, kpad, out, rl, hdr + 1, L.rcap, hdr, st);
     if (rc) return rc;
+    prof_end(st);
   }
   allpairs_refine_kernel<<<sm_count() * 4, 256, 0, st>>>(X32, G, n_frames, n_atoms, kpad, rl, hdr + 1, L.rcap, out);
   GB_CUDA_TRY(cudaGetLastError(), "launch allpairs_refine_kernel");

@@ -72,7 +72,10 @@ __device__ __forceinline__ float qcp_msd_f32(const float (&m)[9], float ga, floa
 }
 
 // Writes the pair's rmsd to both triangles (i < j) or 0 on the diagonal and
-// queues near-identical pairs for refinement.
+// queues pairs the FP32 QCP cannot resolve for exact refinement.  The error
+// of M (split-BF16 or FP32 accumulation) is ~1e-6 * scale / sqrt(n) in msd
+// units, i.e. <= 2e-5 nm in rmsd above r = 0.25 * scale / sqrt(n) (scale =
+// (Ga + Gb) / 2n in nm^2); below it the pair is recomputed.
 __device__ __forceinline__ void pair_epilogue(int64_t i, int64_t j, const float (&m)[9], const double* __restrict__ G,
                                               float inv_n, int64_t F, float* __restrict__ out, PairRefine* rl,
                                               int* rc, int rcap, int* err) {
@@ -86,7 +89,7 @@ __device__ __forceinline__ void pair_epilogue(int64_t i, int64_t j, const float 
   out[i * F + j] = r;
   out[j * F + i] = r;
   const float scale = 0.5f * (ga + gb) * inv_n;
-  if (r < 0.02f * scale) {
+  if (r < 0.25f * scale * sqrtf(inv_n)) {
     const int slot = atomicAdd(rc, 1);
     if (slot < rcap)
       rl[slot] = PairRefine{(int32_t)i, (int32_t)j};

@@ -23,6 +23,10 @@ int sm_count();
 // Maximum opt-in dynamic shared memory per block of the current device.
 int max_dyn_smem();
 
+// Event timing of the dominant kernel of a call (gbrmsd_profile_enable).
+void prof_begin(cudaStream_t st);
+void prof_end(cudaStream_t st);
+
 __host__ __device__ inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
 inline bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }

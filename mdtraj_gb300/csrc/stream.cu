@@ -989,9 +989,9 @@ int32_t rmsd_splits_max(int64_t F, int32_t A) {
   return choose_splits(F, (A + 3) / 4, gw);
 }
 
-// Optional CUDA-event timing of the streaming kernel (the dominant kernel):
-// one event pair per gbrmsd_rmsd_to_reference call, recorded on its launch
-// stream, kept in a ring of up to kProfMax calls.
+// Optional CUDA-event timing of the dominant kernel of each profiled call
+// (streaming kernel, all-pairs tile kernel, ...): one event pair per call,
+// recorded on its launch stream, kept in a ring of up to kProfMax calls.
 namespace {
 constexpr int kProfMax = 4096;
 int g_prof_cap = 0;
@@ -999,11 +999,11 @@ int g_prof_n = 0;
 cudaEvent_t g_ev[kProfMax][2];
 }  // namespace
 
-static void prof_begin(cudaStream_t st) {
+void prof_begin(cudaStream_t st) {
   if (g_prof_n < g_prof_cap) cudaEventRecord(g_ev[g_prof_n][0], st);
 }
 
-static void prof_end(cudaStream_t st) {
+void prof_end(cudaStream_t st) {
   if (g_prof_n < g_prof_cap) {
     cudaEventRecord(g_ev[g_prof_n][1], st);
     ++g_prof_n;
