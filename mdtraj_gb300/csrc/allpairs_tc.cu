@@ -5,18 +5,26 @@
 // (the lo.lo^T term is ~2^-18 relative and dropped).  One tile is a
 // 128 x 240 block of P: 42 frames (126 rows + 2 ignored) by 80 frames.
 //
-// Persistent CTAs (one per SM), 192 threads:
+// The tensor core's FP32 accumulator loses a fraction of an ulp per add in
+// one direction; over the 384 accumulation steps of a 2,048-atom tile that
+// biases msd by ~1e-4 nm^2.  Each 64-atom k block therefore accumulates into
+// a fresh TMEM buffer (12 MMAs), and CUDA-core warps fold the buffer into FP32
+// registers with round-to-nearest adds (the promotion of partial sums used for
+// low-precision tensor GEMMs), which shrinks the bias ~32-fold.
+//
+// Persistent CTAs (one per SM), 448 threads:
 //   warp 0       TMA producer: per 64-atom k block, four 2-D tensor copies
 //                (A_hi, A_lo 128 x 64; B_hi, B_lo 240 x 64; 128-byte swizzle)
 //                into a 2-stage shared-memory ring;
-//   warp 1       allocates 512 TMEM columns (two 240-column accumulators),
-//                one lane issues 12 tcgen05.mma per k block (3 products x 4
-//                k-steps of 16), commits stage releases and accumulator-full
-//                to mbarriers;
-//   warps 2..5   epilogue: tcgen05.ld 48-column chunks (16 frames) into
-//                registers, stage them in shared memory, FP32 QCP per pair
-//                (allpairs.cuh), write both triangles; release the
-//                accumulator so the next tile's MMAs overlap this epilogue.
+//   warp 1       allocates 512 TMEM columns (two 240-column k-block
+//                buffers); one lane issues 12 tcgen05.mma per k block (3
+//                products x 4 k-steps of 16) and commits the stage release and
+//                the buffer-full signal to mbarriers;
+//   warps 2..13  accumulators + epilogue: warp w owns TMEM lanes 32*(w%4).. and
+//                80 of the 240 columns; it folds every k-block buffer into 80
+//                registers, then stages the tile in 48-column chunks (16
+//                frames) through shared memory, solves QCP per pair in FP32
+//                (allpairs.cuh) and writes both triangles.
 // Every wait is bounded; on a timeout the thread records an error and leaves
 // its loop, and the CTA frees its tensor memory before exiting.
 #include <cuda.h>
@@ -45,8 +53,12 @@ constexpr int EPI_COLS = 48;            // 16 frames per epilogue chunk
 constexpr int EPI_LD = EPI_COLS + 1;
 constexpr int EPI_BYTES = TILE_M * EPI_LD * 4;
 constexpr int TMEM_COLS = 512;
-constexpr int ACC_STRIDE = 256;         // TMEM columns between the two accumulators
-constexpr int NTHREADS = 192;
+constexpr int ACC_STRIDE = 256;         // TMEM columns between the two k-block buffers
+constexpr int NGROUP = 3;               // column groups per TMEM lane slice
+constexpr int GCOLS = TILE_N / NGROUP;  // 80 accumulator registers per thread
+constexpr int NEPI = 4 * NGROUP;        // accumulator / epilogue warps
+constexpr int NEPI_THREADS = 32 * NEPI;
+constexpr int NTHREADS = 64 + NEPI_THREADS;
 constexpr uint32_t SPIN = 1u << 24;
 
 // smem: [stages | epilogue staging | barriers | tmem address]
@@ -161,11 +173,12 @@ __global__ void __launch_bounds__(NTHREADS, 1) allpairs_tc_kernel(const __grid_c
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   float* sD = reinterpret_cast<float*>(smem + SMEM_EPI);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + SMEM_BAR);
-  uint64_t* full = bars;                 // [NSTAGE]
-  uint64_t* empty = bars + NSTAGE;       // [NSTAGE]
-  uint64_t* accfull = bars + 2 * NSTAGE; // [2]
-  uint64_t* accempty = accfull + 2;      // [2]
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accempty + 2);
+  uint64_t* full = bars;                  // [NSTAGE] operands landed
+  uint64_t* empty = bars + NSTAGE;        // [NSTAGE] operands consumed by the MMAs
+  uint64_t* kfull = bars + 2 * NSTAGE;    // [2] k-block buffer written
+  uint64_t* kempty = kfull + 2;           // [2] k-block buffer folded by all accumulator warps
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(kempty + 2);
+  volatile int* fail_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
@@ -176,9 +189,10 @@ __global__ void __launch_bounds__(NTHREADS, 1) allpairs_tc_kernel(const __grid_c
       mbar_init(&empty[s], 1);
     }
     for (int b = 0; b < 2; ++b) {
-      mbar_init(&accfull[b], 1);
-      mbar_init(&accempty[b], 4);
+      mbar_init(&kfull[b], 1);
+      mbar_init(&kempty[b], NEPI);
     }
+    *fail_flag = 0;
     fence_mbar_init();
   }
   if (warp == 1) {
@@ -192,8 +206,6 @@ __global__ void __launch_bounds__(NTHREADS, 1) allpairs_tc_kernel(const __grid_c
 
   const int64_t n_tiles = args.n_tiles;
   const int nkb = args.kpad / KBLK;
-  const int64_t rows_total = 3 * args.F;
-  (void)rows_total;
 
   if (warp == 0) {
     // ---------------- TMA producer ----------------
@@ -215,87 +227,94 @@ __global__ void __launch_bounds__(NTHREADS, 1) allpairs_tc_kernel(const __grid_c
           tma_load_2d(st + 2 * A_BYTES + B_BYTES, &map_lo_b, kb * KBLK, row_b, &full[s]);
         }
       }
-      // drain: the last use of every stage must be consumed before the CTA exits
-      for (uint32_t k = (it > NSTAGE ? it - NSTAGE : 0); k < it; ++k) {
-        const int s = k % NSTAGE;
-        if (!wait_bar(&empty[s], (k / NSTAGE) & 1, args.err)) break;
-      }
+      // the last use of every stage must be consumed before the CTA exits
+      for (uint32_t k = (it > NSTAGE ? it - NSTAGE : 0); k < it; ++k)
+        if (!wait_bar(&empty[k % NSTAGE], (k / NSTAGE) & 1, args.err)) break;
     }
   } else if (warp == 1) {
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
       constexpr uint32_t idesc = make_idesc(TILE_M, TILE_N);
-      uint32_t it = 0, tcount = 0;
+      uint32_t it = 0;  // k blocks issued (= k-block buffers used)
       bool ok = true;
-      for (int64_t t = blockIdx.x; t < n_tiles && ok; t += gridDim.x, ++tcount) {
-        const int b = tcount & 1;
-        const uint32_t buse = tcount >> 1;
-        if (buse > 0 && !wait_bar(&accempty[b], (buse - 1) & 1, args.err)) { ok = false; break; }
-        tc_fence_after();
-        const uint32_t d_tmem = tmem_base + b * ACC_STRIDE;
+      for (int64_t t = blockIdx.x; t < n_tiles && ok; t += gridDim.x) {
         for (int kb = 0; kb < nkb; ++kb, ++it) {
+          const int b = it & 1;
+          const uint32_t buse = it >> 1;
+          if (buse > 0 && !wait_bar(&kempty[b], (buse - 1) & 1, args.err)) { ok = false; break; }
           const int s = it % NSTAGE;
           if (!wait_bar(&full[s], (it / NSTAGE) & 1, args.err)) { ok = false; break; }
           tc_fence_after();
+          const uint32_t d_tmem = tmem_base + b * ACC_STRIDE;
           const uint32_t st = smem_addr(smem + s * STAGE_BYTES);
           const uint32_t a_hi = st, a_lo = st + A_BYTES, b_hi = st + 2 * A_BYTES, b_lo = st + 2 * A_BYTES + B_BYTES;
 #pragma unroll
           for (int ks = 0; ks < KBLK / 16; ++ks) {
             const uint32_t koff = ks * 32;  // 16 BF16 = 32 bytes inside the 128-byte swizzle row
-            const uint32_t acc0 = (kb > 0 || ks > 0) ? 1u : 0u;
-            tc_mma(d_tmem, smem_desc_sw128(a_hi + koff), smem_desc_sw128(b_hi + koff), idesc, acc0);
+            tc_mma(d_tmem, smem_desc_sw128(a_hi + koff), smem_desc_sw128(b_hi + koff), idesc, ks > 0 ? 1u : 0u);
             tc_mma(d_tmem, smem_desc_sw128(a_hi + koff), smem_desc_sw128(b_lo + koff), idesc, 1u);
             tc_mma(d_tmem, smem_desc_sw128(a_lo + koff), smem_desc_sw128(b_hi + koff), idesc, 1u);
           }
-          tc_commit(&empty[s]);  // stage reusable once these MMAs have read it
+          tc_commit(&empty[s]);  // operand stage reusable once these MMAs have read it
+          tc_commit(&kfull[b]);  // k-block buffer ready for the accumulator warps
         }
-        if (!ok) break;
-        tc_commit(&accfull[b]);  // accumulator complete
       }
-      // wait for the last commits so no MMA is in flight when TMEM is freed
-      if (tcount > 0) {
-        const uint32_t lt = tcount - 1;
-        wait_bar(&accfull[lt & 1], (lt >> 1) & 1, args.err);
-      }
+      if (it > 0) wait_bar(&kfull[(it - 1) & 1], ((it - 1) >> 1) & 1, args.err);  // no MMA left in flight
     }
   } else {
-    // ---------------- epilogue (warps 2..5) ----------------
-    const int ew = warp - 2;                 // 0..3
-    const int slice = warp & 3;              // TMEM lanes [32*slice, 32*slice + 32)
-    const int row = slice * 32 + lane;       // accumulator row of this thread
-    const int etid = ew * 32 + lane;         // 0..127
+    // ---------------- accumulators + epilogue (warps 2..13) ----------------
+    const int ew = warp - 2;              // 0 .. NEPI-1
+    const int slice = warp & 3;           // TMEM lanes [32*slice, 32*slice + 32)
+    const int grp = ew >> 2;              // column group: columns [80*grp, 80*grp + 80)
+    const int row = slice * 32 + lane;    // accumulator row of this thread
+    const int etid = ew * 32 + lane;      // 0 .. NEPI_THREADS-1
     const float inv_n = 1.0f / (float)args.A;
-    volatile int* go = reinterpret_cast<volatile int*>(tmem_slot + 1);
-    uint32_t tcount = 0;
-    for (int64_t t = blockIdx.x; t < n_tiles; t += gridDim.x, ++tcount) {
-      const int b = tcount & 1;
-      const uint32_t buse = tcount >> 1;
-      // one thread waits; the four epilogue warps then agree on the outcome
-      if (etid == 0) *go = wait_bar(&accfull[b], buse & 1, args.err) ? 1 : 0;
-      named_bar(1, 128);
-      const int proceed = *go;
-      named_bar(1, 128);
+    const uint32_t lane_off = (uint32_t)(slice * 32) << 16;
+    uint32_t it = 0;
+    bool ok = true;
+    for (int64_t t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+      float acc[GCOLS];
+#pragma unroll
+      for (int q = 0; q < GCOLS; ++q) acc[q] = 0.f;
+      for (int kb = 0; kb < nkb; ++kb, ++it) {
+        const int b = it & 1;
+        if (ok && !wait_bar(&kfull[b], (it >> 1) & 1, args.err)) {
+          ok = false;
+          *fail_flag = 1;
+        }
+        if (ok) {
+          tc_fence_after();
+          const uint32_t taddr = tmem_base + (uint32_t)(b * ACC_STRIDE + grp * GCOLS) + lane_off;
+#pragma unroll
+          for (int c0 = 0; c0 < GCOLS; c0 += 16) {
+            float v[16];
+            tc_ld16(taddr + c0, v);
+            tc_wait_ld();
+#pragma unroll
+            for (int q = 0; q < 16; ++q) acc[c0 + q] += v[q];
+          }
+          tc_fence_before();
+        }
+        __syncwarp();
+        if (ok && lane == 0) mbar_arrive(&kempty[b]);
+      }
+      // the whole tile is in registers: stage it 48 columns (16 frames) at a time
+      named_bar(1, NEPI_THREADS);
+      const bool proceed = *fail_flag == 0;
+      named_bar(1, NEPI_THREADS);
       if (!proceed) break;
-      tc_fence_after();
       const int2 tl = args.tiles[t];
       const int64_t i0 = (int64_t)tl.x * FR_M, j0 = (int64_t)tl.y * FR_N;
       for (int ch = 0; ch < TILE_N / EPI_COLS; ++ch) {
-        const uint32_t taddr =
-            tmem_base + (uint32_t)(b * ACC_STRIDE + ch * EPI_COLS) + ((uint32_t)(slice * 32) << 16);
-        float v0[16], v1[16], v2[16];
-        tc_ld16(taddr, v0);
-        tc_ld16(taddr + 16, v1);
-        tc_ld16(taddr + 32, v2);
-        tc_wait_ld();
+        const int lo = ch * EPI_COLS - grp * GCOLS;  // my column q maps to staging column q - lo
         float* dst = sD + row * EPI_LD;
 #pragma unroll
-        for (int q = 0; q < 16; ++q) {
-          dst[q] = v0[q];
-          dst[16 + q] = v1[q];
-          dst[32 + q] = v2[q];
+        for (int q = 0; q < GCOLS; ++q) {
+          const int c = q - lo;
+          if (c >= 0 && c < EPI_COLS) dst[c] = acc[q];
         }
-        named_bar(1, 128);
-        for (int p = etid; p < FR_M * 16; p += 128) {
+        named_bar(1, NEPI_THREADS);
+        for (int p = etid; p < FR_M * 16; p += NEPI_THREADS) {
           const int li = p >> 4, lj = p & 15;
           const int64_t i = i0 + li, j = j0 + ch * 16 + lj;
           if (i < args.F && j < args.F && i <= j) {
@@ -307,11 +326,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) allpairs_tc_kernel(const __grid_c
             pair_epilogue(i, j, m, args.G, inv_n, args.F, args.out, args.rl, args.rc, args.rcap, args.err);
           }
         }
-        named_bar(1, 128);
+        named_bar(1, NEPI_THREADS);
       }
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&accempty[b]);
     }
   }
 
