@@ -134,6 +134,43 @@ int gbrmsd_allpairs(const float* x, int64_t n_frames, int32_t n_atoms, int32_t n
  * this workspace refined exactly and whether a device error was recorded. */
 int gbrmsd_allpairs_status(const void* ws, int32_t* refined_pairs, void* stream);
 
+/* ---- Ragged batch: many trajectories in one launch -------------------------
+ * Each segment s is a trajectory of seg_frames[s] frames of seg_atoms[s] atoms
+ * (padded to seg_padded[s], a multiple of 4), atom-major, starting at float
+ * offset seg_x_offsets[s] (multiple of 4) of one packed device buffer, scored
+ * against its own frame 0 -- the work of `[md.rmsd(t, t, 0) for t in trajs]`
+ * (_rmsd.pyx:211-224 per trajectory).  Output: one float per frame, segments
+ * concatenated in order.
+ *   gbrmsd_ragged_plan   host only: validates the segments, picks the launch
+ *                        configuration (config in [0, gbrmsd_ragged_config_count()),
+ *                        max_unit_quads = largest work unit in 4-atom quads;
+ *                        <= 0 picks defaults) and sizes the workspace;
+ *   gbrmsd_ragged_setup  uploads the segment tables and prepares every
+ *                        segment's reference (synchronises `stream`);
+ *   gbrmsd_ragged_rmsd   one persistent launch + QCP finish + refinement;
+ *                        kernels and a memset only, so it can be captured in
+ *                        a CUDA graph and replayed.
+ */
+typedef struct gbrmsd_ragged_plan {
+  int32_t n_seg;
+  int32_t config;
+  int32_t max_unit_quads;
+  int32_t grid;
+  int64_t total_frames;
+  int64_t total_units;
+  size_t ws_bytes;
+} gbrmsd_ragged_plan_t;
+
+int gbrmsd_ragged_config_count(void);
+int gbrmsd_ragged_plan(const int64_t* seg_x_offsets, const int32_t* seg_atoms, const int32_t* seg_padded,
+                       const int64_t* seg_frames, int32_t n_seg, int32_t config, int32_t max_unit_quads,
+                       gbrmsd_ragged_plan_t* plan);
+int gbrmsd_ragged_setup(const float* x, const int64_t* seg_x_offsets, const int32_t* seg_atoms,
+                        const int32_t* seg_padded, const int64_t* seg_frames, const gbrmsd_ragged_plan_t* plan,
+                        void* ws, size_t ws_bytes, void* stream);
+int gbrmsd_ragged_rmsd(const float* x, float* out, const gbrmsd_ragged_plan_t* plan, void* ws, size_t ws_bytes,
+                       void* stream);
+
 /* ---- In-place centring ------------------------------------------------------
  * Replaces inplace_center_and_trace_atom_major (mdtraj/rmsd/include/center.h:7-8;
  * src/center_generic.h:3-44) for whole trajectories on the device, i.e. the

@@ -14,7 +14,8 @@ from . import _lib  # loads libgbrmsd.so (raises ImportError if it was not built
 from . import _rmsd
 from ._rmsd import rmsd
 from .allpairs import allpairs_rmsd
+from .ragged import RaggedBatch, ragged_rmsd
 from .trajectory import Trajectory
 
-__all__ = ["rmsd", "allpairs_rmsd", "Trajectory", "_rmsd"]
+__all__ = ["rmsd", "allpairs_rmsd", "ragged_rmsd", "RaggedBatch", "Trajectory", "_rmsd"]
 __version__ = "0.1.0"

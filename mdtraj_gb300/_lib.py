@@ -52,6 +52,10 @@ SIGNATURES: dict[str, tuple] = {
     "gbrmsd_allpairs_workspace_bytes": (_sz, [_i64, _i32]),
     "gbrmsd_allpairs": (C.c_int, [_vp, _i64, _i32, _i32, _i64, _i32, _i32, _i32, _vp, _vp, _sz, _vp]),
     "gbrmsd_allpairs_status": (C.c_int, [_vp, _vp, _vp]),
+    "gbrmsd_ragged_config_count": (C.c_int, []),
+    "gbrmsd_ragged_plan": (C.c_int, [_vp, _vp, _vp, _vp, _i32, _i32, _i32, _vp]),
+    "gbrmsd_ragged_setup": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
+    "gbrmsd_ragged_rmsd": (C.c_int, [_vp, _vp, _vp, _vp, _sz, _vp]),
     "gbrmsd_center_inplace": (C.c_int, [_vp, _i64, _i32, _i32, _i64, _i32, _vp, _vp, _vp, _sz, _vp]),
     "gbrmsd_workspace_status": (C.c_int, [_vp, _vp]),
     "gbrmsd_stream_config_count": (C.c_int, []),
@@ -65,6 +69,13 @@ SIGNATURES: dict[str, tuple] = {
     "gbrmsd_copy_rows_kernel": (C.c_int, [_vp, _i64, _vp, _i64, _i64, _i64, _i64, _vp]),
     "gbrmsd_write_centred": (C.c_int, [_vp, _vp, _i64, _vp, _i64, _i32, _vp]),
 }
+
+
+class RaggedPlan(C.Structure):
+    """gbrmsd_ragged_plan_t (include/gbrmsd.h)."""
+
+    _fields_ = [("n_seg", C.c_int32), ("config", C.c_int32), ("max_unit_quads", C.c_int32), ("grid", C.c_int32),
+                ("total_frames", C.c_int64), ("total_units", C.c_int64), ("ws_bytes", C.c_size_t)]
 
 
 class GbrmsdError(RuntimeError):

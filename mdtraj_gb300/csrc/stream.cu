@@ -35,122 +35,22 @@
 #include "common.cuh"
 #include "qcp.cuh"
 #include "stream.cuh"
+#include "stream_dev.cuh"
 
 namespace gb {
 
 namespace {
 
-constexpr int HDR_BYTES = 256;  // workspace header: err word, refine count
-
-struct WsHeader {
-  int err;
-  int refine_count;
-};
-
 // ---------------------------------------------------------------------------
 // Reference preparation (one CTA)
 // ---------------------------------------------------------------------------
-
-constexpr int PREP_THREADS = 1024;
-
-__device__ double block_sum_d(double v, double* red) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  v = warp_sum_d(v);
-  __syncthreads();
-  if (lane == 0) red[warp] = v;
-  __syncthreads();
-  double t = 0.0;
-  if (warp == 0) {
-    t = (lane < (int)(blockDim.x >> 5)) ? red[lane] : 0.0;
-    t = warp_sum_d(t);
-    if (lane == 0) red[0] = t;
-  }
-  __syncthreads();
-  t = red[0];
-  __syncthreads();
-  return t;
-}
 
 __global__ void __launch_bounds__(PREP_THREADS) ref_prepare_kernel(
     const float* __restrict__ raw, int32_t A, int32_t Ap, int32_t layout, int32_t centre,
     float* __restrict__ out, RefInfo* __restrict__ info, double* __restrict__ prefix) {
   __shared__ double red[32];
   __shared__ double part[PREP_THREADS * 3];
-  const int tid = threadIdx.x;
-  // 1. centroid: double accumulation, rounded to float (center_generic.h:19-29)
-  float mu[3] = {0.f, 0.f, 0.f};
-  if (centre) {
-    double s[3] = {0.0, 0.0, 0.0};
-    for (int k = tid; k < A; k += blockDim.x)
-      for (int c = 0; c < 3; ++c) s[c] += (double)raw[3 * k + c];
-    for (int c = 0; c < 3; ++c) {
-      const double t = block_sum_d(s[c], red);
-      mu[c] = (float)(t / (double)A);
-    }
-  }
-  // 2. centred (float subtraction) reference in the requested layout
-  double g = 0.0, sb[3] = {0.0, 0.0, 0.0};
-  for (int k = tid; k < Ap; k += blockDim.x) {
-    for (int c = 0; c < 3; ++c) {
-      float v = 0.f;
-      if (k < A) v = __fsub_rn(raw[3 * k + c], mu[c]);
-      if (layout == ATOM_MAJOR)
-        out[3 * (size_t)k + c] = v;
-      else
-        out[(size_t)c * Ap + k] = v;
-      g += (double)v * (double)v;
-      sb[c] += (double)v;
-    }
-  }
-  g = block_sum_d(g, red);
-  for (int c = 0; c < 3; ++c) sb[c] = block_sum_d(sb[c], red);
-  // 3. prefix sums over quads (for splitting frames across warps)
-  const int Q = (A + 3) >> 2;
-  const int per = (Q + PREP_THREADS - 1) / PREP_THREADS;
-  const int q_lo = min(Q, tid * per), q_hi = min(Q, q_lo + per);
-  double loc[3] = {0.0, 0.0, 0.0};
-  for (int q = q_lo; q < q_hi; ++q)
-    for (int t = 0; t < 4; ++t) {
-      const int k = 4 * q + t;
-      if (k < A)
-        for (int c = 0; c < 3; ++c) loc[c] += (double)__fsub_rn(raw[3 * k + c], mu[c]);
-    }
-  for (int c = 0; c < 3; ++c) part[3 * tid + c] = loc[c];
-  __syncthreads();
-  if (tid == 0) {
-    double run[3] = {0.0, 0.0, 0.0};
-    for (int t = 0; t < PREP_THREADS; ++t)
-      for (int c = 0; c < 3; ++c) {
-        const double v = part[3 * t + c];
-        part[3 * t + c] = run[c];
-        run[c] += v;
-      }
-  }
-  __syncthreads();
-  double run[3] = {part[3 * tid], part[3 * tid + 1], part[3 * tid + 2]};
-  for (int q = q_lo; q < q_hi; ++q) {
-    for (int c = 0; c < 3; ++c) prefix[3 * (size_t)q + c] = run[c];
-    for (int t = 0; t < 4; ++t) {
-      const int k = 4 * q + t;
-      if (k < A)
-        for (int c = 0; c < 3; ++c) run[c] += (double)__fsub_rn(raw[3 * k + c], mu[c]);
-    }
-  }
-  if (q_lo < q_hi && q_hi == Q)
-    for (int c = 0; c < 3; ++c) prefix[3 * (size_t)Q + c] = run[c];
-  if (Q == 0 && tid == 0)
-    for (int c = 0; c < 3; ++c) prefix[c] = 0.0;
-  if (tid == 0) {
-    info->g = g;
-    for (int c = 0; c < 3; ++c) {
-      info->sum[c] = sb[c];
-      info->centroid[c] = mu[c];
-    }
-    info->n_atoms = A;
-    info->n_padded = Ap;
-    info->layout = layout;
-    info->centred = centre;
-  }
+  prepare_reference_block(raw, A, Ap, layout, centre, out, info, prefix, red, part);
 }
 
 // ---------------------------------------------------------------------------
@@ -191,12 +91,6 @@ __device__ __forceinline__ bool cursor_next(Cursor& cur, int64_t W, int32_t S, i
   return false;
 }
 
-// Axis-major stages are a sequence of 64-quad boxes [x 256 | y 256 | z 256]
-// (3 KB), each moved by one 3-D tensor copy of the box (256 atoms, 3 axes, 1
-// frame); atom-major stages are one contiguous 1-D bulk copy.
-constexpr int BOX_QUADS = 64;
-constexpr int BOX_BYTES = BOX_QUADS * 48;
-
 template <int LAYOUT, int CQ>
 __device__ __forceinline__ void issue_chunk(const StreamArgs& p, const void* tmap, const Cursor& cur,
                                             unsigned char* stage, uint64_t* bar) {
@@ -211,98 +105,6 @@ __device__ __forceinline__ void issue_chunk(const StreamArgs& p, const void* tma
     mbar_arrive_expect_tx(bar, (uint32_t)(nbox * BOX_BYTES));
     for (int b = 0; b < nbox; ++b)
       tma_load_3d(stage + b * BOX_BYTES, tmap, 4 * (qb + b * BOX_QUADS), 0, (int32_t)cur.frame, bar);
-  }
-}
-
-// Loads quad i of a stage (or of the reference) as x[4], y[4], z[4].
-template <int LAYOUT, int CQ>
-__device__ __forceinline__ void load_stage_quad(const float* st, int i, float (&x)[4], float (&y)[4],
-                                                float (&z)[4]) {
-  if (LAYOUT == ATOM_MAJOR) {
-    const float4 t0 = lds4(st + 12 * i), t1 = lds4(st + 12 * i + 4), t2 = lds4(st + 12 * i + 8);
-    x[0] = t0.x; y[0] = t0.y; z[0] = t0.z; x[1] = t0.w;
-    y[1] = t1.x; z[1] = t1.y; x[2] = t1.z; y[2] = t1.w;
-    z[2] = t2.x; x[3] = t2.y; y[3] = t2.z; z[3] = t2.w;
-  } else {
-    const float* b = st + (i / BOX_QUADS) * (BOX_BYTES / 4) + 4 * (i % BOX_QUADS);
-    const float4 tx = lds4(b), ty = lds4(b + 4 * BOX_QUADS), tz = lds4(b + 8 * BOX_QUADS);
-    x[0] = tx.x; x[1] = tx.y; x[2] = tx.z; x[3] = tx.w;
-    y[0] = ty.x; y[1] = ty.y; y[2] = ty.z; y[3] = ty.w;
-    z[0] = tz.x; z[1] = tz.y; z[2] = tz.z; z[3] = tz.w;
-  }
-}
-
-template <int LAYOUT, bool SMEM>
-__device__ __forceinline__ void load_ref_quad(const float* ref, int32_t Ap, int32_t gq, float (&x)[4],
-                                              float (&y)[4], float (&z)[4]) {
-  float4 t0, t1, t2;
-  if (LAYOUT == ATOM_MAJOR) {
-    const float* q = ref + (size_t)gq * 12;
-    if (SMEM) { t0 = lds4(q); t1 = lds4(q + 4); t2 = lds4(q + 8); }
-    else { t0 = ldg4(q); t1 = ldg4(q + 4); t2 = ldg4(q + 8); }
-    x[0] = t0.x; y[0] = t0.y; z[0] = t0.z; x[1] = t0.w;
-    y[1] = t1.x; z[1] = t1.y; x[2] = t1.z; y[2] = t1.w;
-    z[2] = t2.x; x[3] = t2.y; y[3] = t2.z; z[3] = t2.w;
-  } else {
-    const float* q = ref + (size_t)gq * 4;
-    if (SMEM) { t0 = lds4(q); t1 = lds4(q + Ap); t2 = lds4(q + 2 * (size_t)Ap); }
-    else { t0 = ldg4(q); t1 = ldg4(q + Ap); t2 = ldg4(q + 2 * (size_t)Ap); }
-    x[0] = t0.x; x[1] = t0.y; x[2] = t0.z; x[3] = t0.w;
-    y[0] = t1.x; y[1] = t1.y; y[2] = t1.z; y[3] = t1.w;
-    z[0] = t2.x; z[1] = t2.y; z[2] = t2.z; z[3] = t2.w;
-  }
-}
-
-// Number of level-1 sums per mode.
-template <int MODE>
-struct NSums {
-  static constexpr int value = MODE == MODE_CENTER ? 13 : MODE == MODE_PRECENTERED ? 9 : MODE == MODE_NOSUPERPOSE ? 1 : 3;
-};
-
-// Level-1 accumulation of one quad (4 atoms).  MASKED handles the last quad
-// of a frame whose atom count is not a multiple of 4 (nv valid atoms).
-template <int MODE, bool MASKED, int NV>
-__device__ __forceinline__ void accum_quad(float (&acc)[NV], const float (&ax)[4], const float (&ay)[4],
-                                           const float (&az)[4], const float (&bx)[4], const float (&by)[4],
-                                           const float (&bz)[4], const float (&shift)[3], int nv) {
-#pragma unroll
-  for (int t = 0; t < 4; ++t) {
-    float dx, dy, dz;
-    if constexpr (MODE == MODE_CENTER) {
-      dx = ax[t] - shift[0]; dy = ay[t] - shift[1]; dz = az[t] - shift[2];
-    } else if constexpr (MODE == MODE_NOSUPERPOSE) {
-      dx = ax[t] - bx[t]; dy = ay[t] - by[t]; dz = az[t] - bz[t];
-    } else {
-      dx = ax[t]; dy = ay[t]; dz = az[t];
-    }
-    if constexpr (MASKED) {
-      if (t >= nv) { dx = 0.f; dy = 0.f; dz = 0.f; }
-    }
-    if constexpr (MODE == MODE_NOSUPERPOSE) {
-      acc[0] = fmaf(dx, dx, acc[0]);
-      acc[0] = fmaf(dy, dy, acc[0]);
-      acc[0] = fmaf(dz, dz, acc[0]);
-    } else {
-      acc[0] = fmaf(dx, bx[t], acc[0]);
-      acc[1] = fmaf(dx, by[t], acc[1]);
-      acc[2] = fmaf(dx, bz[t], acc[2]);
-      acc[3] = fmaf(dy, bx[t], acc[3]);
-      acc[4] = fmaf(dy, by[t], acc[4]);
-      acc[5] = fmaf(dy, bz[t], acc[5]);
-      acc[6] = fmaf(dz, bx[t], acc[6]);
-      acc[7] = fmaf(dz, by[t], acc[7]);
-      acc[8] = fmaf(dz, bz[t], acc[8]);
-      if constexpr (MODE == MODE_CENTER) {
-        acc[9] += dx;
-        acc[10] += dy;
-        acc[11] += dz;
-        float gg = acc[12];
-        gg = fmaf(dx, dx, gg);
-        gg = fmaf(dy, dy, gg);
-        gg = fmaf(dz, dz, gg);
-        acc[12] = gg;
-      }
-    }
   }
 }
 
@@ -531,107 +333,20 @@ __global__ void __launch_bounds__(WARPS * 32, 1) stream_kernel(const StreamArgs 
 __global__ void __launch_bounds__(256) finish_kernel(const FinishArgs a) {
   const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= a.n_frames) return;
-  const int32_t A = a.n_atoms;
-  const int32_t S = a.splits;
-  const int32_t Q = (A + 3) >> 2;
-  const double* base = a.sums + f * (int64_t)S * SUMS_STRIDE;
-  const double dA = (double)A;
-
-  if (a.mode == MODE_NOSUPERPOSE) {
-    double g = 0.0;
-    for (int j = 0; j < S; ++j) g += base[j * SUMS_STRIDE + 12];
-    double msd = g / dA;
-    if (!(msd > 0.0)) msd = 0.0;
-    a.out_rmsd[f] = (float)sqrt(msd);
-    return;
-  }
-  if (a.mode == MODE_TRACE) {
-    for (int c = 0; c < 3; ++c) {
-      double s = 0.0;
-      for (int j = 0; j < S; ++j) s += base[j * SUMS_STRIDE + 9 + c];
-      a.out_centroid[3 * f + c] = (float)(s / dA);
-    }
-    return;
-  }
-
-  double m[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-  double ga, gb, mu[3] = {0.0, 0.0, 0.0};
-  if (a.mode == MODE_PRECENTERED) {
-    for (int j = 0; j < S; ++j)
-      for (int i = 0; i < 9; ++i) m[i] += base[j * SUMS_STRIDE + i];
-    ga = (double)a.g_target[f];
-    gb = (double)a.g_ref_override;
-  } else {
-    // Exact re-centring of the shifted partial sums (FP64):
-    //   mu = sum_j (sd_j + n_j s_j) / A
-    //   Ga = sum_j (g_j + 2 (s_j - mu) . sd_j + n_j |s_j - mu|^2)
-    //   M  = sum_j (m_j + (s_j - mu) B_j^T),  B_j = sum of reference over split j
-    double sa[3] = {0.0, 0.0, 0.0};
-    for (int j = 0; j < S; ++j) {
-      const double* r = base + j * SUMS_STRIDE;
-      const int32_t q0 = (int32_t)(((int64_t)j * Q) / S), q1 = (int32_t)(((int64_t)(j + 1) * Q) / S);
-      const double nj = (double)(min(4 * q1, A) - 4 * q0);
-      for (int c = 0; c < 3; ++c) sa[c] += r[9 + c] + nj * r[16 + c];
-    }
-    for (int c = 0; c < 3; ++c) mu[c] = sa[c] / dA;
-    ga = 0.0;
-    for (int j = 0; j < S; ++j) {
-      const double* r = base + j * SUMS_STRIDE;
-      const int32_t q0 = (int32_t)(((int64_t)j * Q) / S), q1 = (int32_t)(((int64_t)(j + 1) * Q) / S);
-      const double nj = (double)(min(4 * q1, A) - 4 * q0);
-      double ds[3], bj[3];
-      for (int c = 0; c < 3; ++c) {
-        ds[c] = r[16 + c] - mu[c];
-        bj[c] = a.ref_prefix[3 * (size_t)q1 + c] - a.ref_prefix[3 * (size_t)q0 + c];
-      }
-      ga += r[12] + 2.0 * (ds[0] * r[9] + ds[1] * r[10] + ds[2] * r[11]) +
-            nj * (ds[0] * ds[0] + ds[1] * ds[1] + ds[2] * ds[2]);
-      for (int i = 0; i < 3; ++i)
-        for (int k = 0; k < 3; ++k) m[3 * i + k] += r[3 * i + k] + ds[i] * bj[k];
-    }
-    gb = a.ref_info->g;
-    if (a.out_centroid)
-      for (int c = 0; c < 3; ++c) a.out_centroid[3 * f + c] = (float)mu[c];
-    if (a.out_trace) a.out_trace[f] = (float)ga;
-  }
-
-  bool self = (f == a.self_index);
-  if (self && a.mode == MODE_PRECENTERED) self = (a.g_target[f] == a.g_ref_override);
-  if (self) {
-    a.out_rmsd[f] = 0.f;
-    return;
-  }
-  bool finite = isfinite(ga) && isfinite(gb);
-  for (int i = 0; i < 9; ++i) finite = finite && isfinite(m[i]);
-  if (!finite) {
-    atomicOr(a.err, DEV_ERR_NONFINITE);
-    a.out_rmsd[f] = nanf("");
-    return;
-  }
-  int iters = 0;
-  const double lam = qcp_lambda_max_mixed(m, ga, gb, &iters);
-  double msd = (ga + gb - 2.0 * lam) / dA;
-  if (!(msd > 0.0)) msd = 0.0;
-  a.out_rmsd[f] = sqrtf((float)msd);
-
-  // One-pass sums resolve msd to about 1e-7 * scale / sqrt(A); below
-  // (0.1 * scale / sqrt(A))^2 the direct residual is recomputed (see
-  // refine_kernel).  scale = (G_a + G_b) / (2 A).
-  const double scale = (ga + gb) / (2.0 * dA);
-  if (msd * dA < 0.01 * scale * scale && A > 0) {
-    double rot[9];
-    qcp_rotation(m, lam, rot);
-    const int slot = atomicAdd(a.refine_count, 1);
-    RefineEntry e;
-    e.frame = f;
-    for (int i = 0; i < 9; ++i) e.rot[i] = (float)rot[i];
-    for (int c = 0; c < 3; ++c) {
-      e.mu_hi[c] = (float)mu[c];
-      e.mu_lo[c] = (float)(mu[c] - (double)e.mu_hi[c]);
-    }
-    e.pad = 0.f;
-    a.refine[slot] = e;
-  }
+  FrameCtx c;
+  c.recs = a.sums + f * (int64_t)a.splits * SUMS_STRIDE;
+  c.S = a.splits;
+  c.A = a.n_atoms;
+  c.mode = a.mode;
+  c.ref_info = a.ref_info;
+  c.ref_prefix = a.ref_prefix;
+  c.g_target = (a.mode == MODE_PRECENTERED) ? a.g_target[f] : 0.f;
+  c.g_ref = a.g_ref_override;
+  c.self = (f == a.self_index);
+  c.out_idx = f;
+  c.refine_frame = f;
+  c.refine_seg = 0;
+  finish_frame(c, a.out_rmsd, a.out_centroid, a.out_trace, a.refine, a.refine_count, a.err);
 }
 
 // ---------------------------------------------------------------------------
@@ -648,46 +363,6 @@ struct RefineArgs {
   const int* count;
   float* out_rmsd;
 };
-
-template <int LAYOUT>
-__device__ __forceinline__ void load_frame_quad(const float* fr, int32_t Ap, int32_t q, float (&x)[4], float (&y)[4],
-                                                float (&z)[4]) {
-  if (LAYOUT == ATOM_MAJOR) {
-    const float4 t0 = ldg4(fr + 12 * (size_t)q), t1 = ldg4(fr + 12 * (size_t)q + 4),
-                 t2 = ldg4(fr + 12 * (size_t)q + 8);
-    x[0] = t0.x; y[0] = t0.y; z[0] = t0.z; x[1] = t0.w;
-    y[1] = t1.x; z[1] = t1.y; x[2] = t1.z; y[2] = t1.w;
-    z[2] = t2.x; x[3] = t2.y; y[3] = t2.z; z[3] = t2.w;
-  } else {
-    const float4 tx = ldg4(fr + 4 * (size_t)q), ty = ldg4(fr + Ap + 4 * (size_t)q),
-                 tz = ldg4(fr + 2 * (size_t)Ap + 4 * (size_t)q);
-    x[0] = tx.x; x[1] = tx.y; x[2] = tx.z; x[3] = tx.w;
-    y[0] = ty.x; y[1] = ty.y; y[2] = ty.z; y[3] = ty.w;
-    z[0] = tz.x; z[1] = tz.y; z[2] = tz.z; z[3] = tz.w;
-  }
-}
-
-// sum over valid atoms of |R (a - mu) - b|^2 for one quad
-__device__ __forceinline__ float residual_quad(const RefineEntry& en, const float (&ax)[4], const float (&ay)[4],
-                                               const float (&az)[4], const float (&bx)[4], const float (&by)[4],
-                                               const float (&bz)[4], int nv) {
-  float part = 0.f;
-#pragma unroll
-  for (int t = 0; t < 4; ++t) {
-    if (t < nv) {
-      const float dx = (ax[t] - en.mu_hi[0]) - en.mu_lo[0];
-      const float dy = (ay[t] - en.mu_hi[1]) - en.mu_lo[1];
-      const float dz = (az[t] - en.mu_hi[2]) - en.mu_lo[2];
-      const float rx = fmaf(en.rot[0], dx, fmaf(en.rot[1], dy, en.rot[2] * dz)) - bx[t];
-      const float ry = fmaf(en.rot[3], dx, fmaf(en.rot[4], dy, en.rot[5] * dz)) - by[t];
-      const float rz = fmaf(en.rot[6], dx, fmaf(en.rot[7], dy, en.rot[8] * dz)) - bz[t];
-      part = fmaf(rx, rx, part);
-      part = fmaf(ry, ry, part);
-      part = fmaf(rz, rz, part);
-    }
-  }
-  return part;
-}
 
 template <int LAYOUT>
 __global__ void __launch_bounds__(256) refine_kernel(const RefineArgs r) {

@@ -32,11 +32,11 @@ struct RefInfo {
 // A frame whose QCP msd is too small for the one-pass sums to resolve; the
 // refinement pass recomputes it as sum |R (a - mu) - b|^2 / n directly.
 struct RefineEntry {
-  int64_t frame;
+  int64_t frame;   // frame index (global frame index on the ragged path)
   float rot[9];
   float mu_hi[3];
   float mu_lo[3];
-  float pad;
+  int32_t seg;     // segment of the frame (ragged path; 0 otherwise)
 };
 
 struct StreamArgs {

@@ -79,8 +79,8 @@ def _torch_rot_from_quat(q):
 
 def device_single_reference(n_frames: int, n_atoms: int, n_padded: int, layout: int, seed: int, device,
                             sigma_lo: float = 0.05, sigma_hi: float = 0.05, exact_fraction: float = 0.0,
-                            cube: float = 4.0, translate: float = 2.0, chunk: int = 2048):
-    """Fills a padded device buffer with single-reference frames.
+                            cube: float = 4.0, translate: float = 2.0, chunk: int = 2048, out=None):
+    """Fills a padded device buffer (new, or `out`) with single-reference frames.
 
     layout 0: (F, n_padded * 3) atom-major; layout 1: (F, 3, n_padded)
     axis-major.  sigma is log-uniform in [sigma_lo, sigma_hi] per frame;
@@ -101,10 +101,13 @@ def device_single_reference(n_frames: int, n_atoms: int, n_padded: int, layout: 
     if exact_fraction > 0 and n_frames > 1:
         k = max(1, int(round(exact_fraction * n_frames)))
         sig[rng.choice(np.arange(1, n_frames), size=min(k, n_frames - 1), replace=False)] = 0.0
-    if layout == 0:
-        out = torch.zeros((n_frames, n_padded * 3), dtype=torch.float32, device=device)
+    if out is None:
+        if layout == 0:
+            out = torch.zeros((n_frames, n_padded * 3), dtype=torch.float32, device=device)
+        else:
+            out = torch.zeros((n_frames, 3, n_padded), dtype=torch.float32, device=device)
     else:
-        out = torch.zeros((n_frames, 3, n_padded), dtype=torch.float32, device=device)
+        out.zero_()
     sig_t = torch.from_numpy(sig).to(device)
     for s in range(0, n_frames, chunk):
         e = min(n_frames, s + chunk)
@@ -176,3 +179,12 @@ def device_metastable_walk(n_frames: int, n_atoms: int, n_padded: int, seed: int
         fr = torch.einsum("fkj,fij->fki", pts, rot).to(torch.float32)
         out[s0:e].view(e - s0, n_padded, 3)[:, :n_atoms, :] = fr
     return labels, out
+
+
+def ragged_shapes(n_seg: int = 512, seed: int = 0, atoms=(50, 20000), frames=(100, 5000)):
+    """Segment shapes of the ragged workload: atom counts log-uniform integers
+    in `atoms`, frame counts uniform integers in `frames` (inclusive)."""
+    rng = np.random.default_rng(seed)
+    a = np.rint(np.exp(rng.uniform(math.log(atoms[0]), math.log(atoms[1]), n_seg))).astype(np.int32)
+    f = rng.integers(frames[0], frames[1] + 1, n_seg).astype(np.int64)
+    return a, f

@@ -125,3 +125,24 @@ def test_trajectory_contract():
     assert t._rmsd_traces is None
     one = md.Trajectory(np.zeros((4, 3)))
     assert one.n_frames == 1 and one.n_atoms == 4
+
+
+def test_autotune_bucket_and_cache_roundtrip(tmp_path, monkeypatch):
+    from mdtraj_gb300 import autotune
+
+    monkeypatch.setenv("MDTRAJ_GB300_CACHE", str(tmp_path))
+    b1 = autotune.shape_bucket([100, 2000, 50], [10, 20, 30])
+    b2 = autotune.shape_bucket([101, 2005, 50], [10, 20, 30])
+    assert b1 == b2 and b1.startswith("ragged:")
+    assert autotune.load_cache() == {}
+    autotune.save_cache({b1: {"config": 2, "max_unit_quads": 256}})
+    assert autotune.load_cache()[b1]["config"] == 2
+
+
+def test_ragged_layout_is_padded_and_aligned():
+    from mdtraj_gb300 import RaggedBatch
+
+    off, padded, total = RaggedBatch.layout([5, 8, 1], [2, 3, 4])
+    assert list(padded) == [8, 8, 4]
+    assert list(off) == [0, 2 * 3 * 8, 2 * 3 * 8 + 3 * 3 * 8]
+    assert all(o % 4 == 0 for o in off) and total == off[-1] + 4 * 3 * 4
