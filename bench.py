@@ -590,7 +590,6 @@ def run_ragged(args) -> dict:
     for _ in range(args.warmup):
         batch.replay()
     torch.cuda.synchronize()
-    lib.gbrmsd_profile_enable(args.steps)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
         e0.record()
@@ -598,10 +597,16 @@ def run_ragged(args) -> dict:
             batch.replay()
         e1.record()
         torch.cuda.synchronize()
+    ms_step = e0.elapsed_time(e1) / args.steps
+    # events recorded inside a captured graph time nothing: the stream kernel's
+    # own duration comes from the same launches issued directly
+    lib.gbrmsd_profile_enable(args.steps)
+    for _ in range(args.steps):
+        batch.run()
+    torch.cuda.synchronize()
     kms = np.zeros(args.steps, dtype=np.float32)
     nk = lib.gbrmsd_profile_read(kms.ctypes.data, args.steps)
     lib.gbrmsd_profile_enable(0)
-    ms_step = e0.elapsed_time(e1) / args.steps
     F_tot = int(frames.sum())
     value = world * F_tot / (ms_step / 1e3)
     k_ms = float(np.mean(kms[:nk])) if nk else float("nan")

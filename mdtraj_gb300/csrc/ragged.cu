@@ -84,43 +84,102 @@ __global__ void __launch_bounds__(PREP_THREADS) ragged_ref_kernel(const float* _
                           reinterpret_cast<double*>(r + ref_prefix_off(sg.n_padded)), red, part);
 }
 
-// One unit of work with everything the consumer needs.
-struct RUnit {
-  int64_t u;
-  const float* fr;
+// Producer cursor over the unit sequence of one warp: units u, u + WARPS,
+// u + 2 WARPS, ... of the CTA's range.  Within a segment units are ordered
+// split-major (unit = unit0 + j * F + f for split j of frame f), so the warps
+// of a CTA stream consecutive frames over the same reference slice and the
+// slice is served from L1.  Stepping is incremental: the binary search over the
+// segment table runs once per warp; afterwards segments are entered by a
+// forward scan, and frame/split advance by additions.
+struct RCursor {
+  int64_t u, uend, seg_uend, unit0, x_seg;
   const float* ref;
-  int32_t A, q0, q1, c;
+  int32_t seg, A, Ap, F, S, Q, f, j, q0, q1, c;
 };
 
-__device__ __forceinline__ void runit_set(RUnit& w, const RaggedArgs& p, int64_t u) {
-  w.u = u;
-  w.c = 0;
-  const int s = find_seg_by_unit(p.segs, p.n_seg, u);
-  const RaggedSeg sg = p.segs[s];
-  const int64_t lu = u - sg.unit0;
-  int64_t f;
-  int32_t j;
-  if (sg.splits == 1) {
-    f = lu;
-    j = 0;
-  } else {
-    f = lu / sg.splits;
-    j = (int32_t)(lu - f * sg.splits);
-  }
-  const int32_t Q = (sg.n_atoms + 3) >> 2;
-  w.q0 = (int32_t)(((int64_t)j * Q) / sg.splits);
-  w.q1 = (int32_t)(((int64_t)(j + 1) * Q) / sg.splits);
-  w.A = sg.n_atoms;
-  w.fr = p.x + sg.x_off + f * 3 * (int64_t)sg.n_padded;
-  w.ref = reinterpret_cast<const float*>(p.ref_base + sg.ref_off + ref_coords_off());
+__device__ __forceinline__ void rc_split_range(RCursor& w) {
+  w.q0 = (int32_t)(((int64_t)w.j * w.Q) / w.S);
+  w.q1 = (int32_t)(((int64_t)(w.j + 1) * w.Q) / w.S);
 }
 
-template <int CQ>
-__device__ __forceinline__ void ragged_issue(const RUnit& w, unsigned char* stage, uint64_t* bar) {
+__device__ __forceinline__ void rc_enter(RCursor& w, const RaggedArgs& p) {
+  const RaggedSeg sg = p.segs[w.seg];
+  w.unit0 = sg.unit0;
+  w.A = sg.n_atoms;
+  w.Ap = sg.n_padded;
+  w.F = sg.n_frames;
+  w.S = sg.splits;
+  w.Q = (sg.n_atoms + 3) >> 2;
+  w.seg_uend = sg.unit0 + (int64_t)sg.splits * sg.n_frames;
+  w.x_seg = sg.x_off;
+  w.ref = reinterpret_cast<const float*>(p.ref_base + sg.ref_off + ref_coords_off());
+  const int64_t lu = w.u - sg.unit0;
+  w.j = (int32_t)(lu / w.F);
+  w.f = (int32_t)(lu - (int64_t)w.j * w.F);
+  rc_split_range(w);
+}
+
+__device__ __forceinline__ void rc_start(RCursor& w, const RaggedArgs& p, int64_t u, int64_t uend) {
+  w.u = u;
+  w.uend = uend;
+  w.c = 0;
+  if (u >= uend) return;
+  w.seg = find_seg_by_unit(p.segs, p.n_seg, u);
+  rc_enter(w, p);
+}
+
+template <int WARPS>
+__device__ __forceinline__ void rc_next_unit(RCursor& w, const RaggedArgs& p) {
+  w.u += WARPS;
+  w.c = 0;
+  if (w.u >= w.uend) return;
+  if (w.u < w.seg_uend) {
+    w.f += WARPS;
+    if (w.f >= w.F) {
+      do { w.f -= w.F; ++w.j; } while (w.f >= w.F);
+      rc_split_range(w);
+    }
+    return;
+  }
+  do { ++w.seg; } while (w.seg + 1 < p.n_seg && p.segs[w.seg + 1].unit0 <= w.u);
+  rc_enter(w, p);
+}
+
+// Per-stage description of the staged chunk, written by the issuing lane
+// before its arrive (release) and read by the warp after the wait (acquire).
+struct ChunkMeta {
+  const float* ref;  // reference quads of the chunk's first quad
+  int64_t rec;       // sums record of the unit
+  int32_t arem;      // atoms from the chunk's first quad to the end of the frame
+  int32_t nq;        // quads in the chunk
+  int32_t flags;     // 1: first chunk of its unit, 2: last chunk of its unit
+  int32_t pad;
+};
+static_assert(sizeof(ChunkMeta) == 32, "ChunkMeta is 32 bytes");
+
+// Issues the cursor's current chunk into `stage` (all lanes advance the
+// cursor; lane 0 writes the metadata and starts the copy).
+template <int CQ, int WARPS>
+__device__ __forceinline__ void rc_issue(RCursor& w, const RaggedArgs& p, int lane, unsigned char* stage,
+                                         ChunkMeta* meta, uint64_t* bar) {
   const int32_t qb = w.q0 + w.c * CQ;
   const int32_t nq = min(CQ, w.q1 - qb);
-  mbar_arrive_expect_tx(bar, (uint32_t)nq * 48u);
-  bulk_g2s(stage, w.fr + (size_t)qb * 12, (uint32_t)nq * 48u, bar);
+  const bool last = qb + nq >= w.q1;
+  if (lane == 0) {
+    ChunkMeta m;
+    m.ref = w.ref + (size_t)qb * 12;
+    m.rec = w.unit0 + (int64_t)w.f * w.S + w.j;
+    m.arem = w.A - 4 * qb;
+    m.nq = nq;
+    m.flags = (w.c == 0 ? 1 : 0) | (last ? 2 : 0);
+    m.pad = 0;
+    *meta = m;
+    fence_proxy_async_smem();
+    mbar_arrive_expect_tx(bar, (uint32_t)nq * 48u);
+    bulk_g2s(stage, p.x + w.x_seg + (int64_t)w.f * 3 * w.Ap + (size_t)qb * 12, (uint32_t)nq * 48u, bar);
+  }
+  if (last) rc_next_unit<WARPS>(w, p);
+  else w.c += 1;
 }
 
 template <int CQ, int NSTAGE, int WARPS>
@@ -133,36 +192,20 @@ __global__ void __launch_bounds__(WARPS * 32, 1) ragged_stream_kernel(const Ragg
   const int warp = threadIdx.x >> 5;
   unsigned char* stages = smem + (size_t)warp * NSTAGE * STAGE_BYTES;
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)WARPS * NSTAGE * STAGE_BYTES) + warp * NSTAGE;
+  ChunkMeta* metas = reinterpret_cast<ChunkMeta*>(smem + (size_t)WARPS * NSTAGE * (STAGE_BYTES + 8)) +
+                     warp * NSTAGE;
   if (lane == 0) {
     for (int s = 0; s < NSTAGE; ++s) mbar_init(&bars[s], 1);
     fence_mbar_init();
   }
   __syncthreads();
 
-  const int64_t ubeg = p.cta_begin[blockIdx.x], uend = p.cta_begin[blockIdx.x + 1];
-  auto next_unit = [&](RUnit& w) -> bool {  // advance to the next chunk; true when a new unit starts
-    w.c += 1;
-    if (w.q0 + w.c * CQ >= w.q1) {
-      const int64_t u = w.u + WARPS;
-      if (u < uend) runit_set(w, p, u); else w.u = uend;
-      return true;
-    }
-    return false;
-  };
-
-  RUnit pc, cc;
-  pc.u = cc.u = uend;
-  if (ubeg + warp < uend) {
-    runit_set(pc, p, ubeg + warp);
-    cc = pc;
-  }
-  int64_t issued = 0, consumed = 0;
-  for (int s = 0; s < NSTAGE; ++s) {
-    if (pc.u < uend) {
-      if (lane == 0) ragged_issue<CQ>(pc, stages + s * STAGE_BYTES, &bars[s]);
-      next_unit(pc);
-      ++issued;
-    }
+  RCursor pc;
+  rc_start(pc, p, p.cta_begin[blockIdx.x] + warp, p.cta_begin[blockIdx.x + 1]);
+  int issued = 0, consumed = 0;
+  for (int s = 0; s < NSTAGE && pc.u < pc.uend; ++s) {
+    rc_issue<CQ, WARPS>(pc, p, lane, stages + s * STAGE_BYTES, &metas[s], &bars[s]);
+    ++issued;
   }
   __syncwarp();
 
@@ -174,31 +217,24 @@ __global__ void __launch_bounds__(WARPS * 32, 1) ragged_stream_kernel(const Ragg
   int pending = 0;
   float shift[3] = {0.f, 0.f, 0.f};
 
-  while (cc.u < uend) {
-    const bool unit_start = (cc.c == 0);
-    if (unit_start) {
-#pragma unroll
-      for (int j = 0; j < NV; ++j) { acc2[j] = cf_zero(); acc1[j] = 0.f; }
-      pending = 0;
-    }
-    const int32_t A = cc.A;
-    const int32_t Q = (A + 3) >> 2;
-    const int32_t qb = cc.q0 + cc.c * CQ;
-    const int32_t nq = min(CQ, cc.q1 - qb);
+  while (consumed < issued) {
     if (!mbar_wait_bounded(&bars[slot], (phases >> slot) & 1u, p.err)) {
       failed = true;
       break;
     }
     phases ^= 1u << slot;
     ++consumed;
+    const ChunkMeta m = metas[slot];
     const float* st = reinterpret_cast<const float*>(stages + slot * STAGE_BYTES);
-
-    if (unit_start) {
+    if (m.flags & 1) {
+#pragma unroll
+      for (int j = 0; j < NV; ++j) { acc2[j] = cf_zero(); acc1[j] = 0.f; }
+      pending = 0;
       float sx = 0.f, sy = 0.f, sz = 0.f, cnt = 0.f;
-      if (lane < nq) {
+      if (lane < m.nq) {
         float xx[4], yy[4], zz[4];
         load_stage_quad<ATOM_MAJOR, CQ>(st, lane, xx, yy, zz);
-        const int nv = A - 4 * (qb + lane);
+        const int nv = m.arem - 4 * lane;
 #pragma unroll
         for (int t = 0; t < 4; ++t)
           if (t < nv) { sx += xx[t]; sy += yy[t]; sz += zz[t]; cnt += 1.f; }
@@ -206,17 +242,16 @@ __global__ void __launch_bounds__(WARPS * 32, 1) ragged_stream_kernel(const Ragg
       sx = warp_sum(sx); sy = warp_sum(sy); sz = warp_sum(sz); cnt = warp_sum(cnt);
       shift[0] = sx / cnt; shift[1] = sy / cnt; shift[2] = sz / cnt;
     }
-    const bool has_tail = ((A & 3) != 0) && (qb + nq == Q);
 #pragma unroll
     for (int kq = 0; kq < QPL; ++kq) {
       const int i = lane + 32 * kq;
-      if (i < nq) {
-        const int32_t gq = qb + i;
+      if (i < m.nq) {
         float ax[4], ay[4], az[4], bx[4], by[4], bz[4];
         load_stage_quad<ATOM_MAJOR, CQ>(st, i, ax, ay, az);
-        load_ref_quad<ATOM_MAJOR, false>(cc.ref, 0, gq, bx, by, bz);
-        if (has_tail && i == nq - 1)
-          accum_quad<MODE_CENTER, true, NV>(acc1, ax, ay, az, bx, by, bz, shift, A - 4 * gq);
+        load_ref_quad<ATOM_MAJOR, false>(m.ref, 0, i, bx, by, bz);
+        const int nv = m.arem - 4 * i;
+        if (nv < 4)
+          accum_quad<MODE_CENTER, true, NV>(acc1, ax, ay, az, bx, by, bz, shift, nv);
         else
           accum_quad<MODE_CENTER, false, NV>(acc1, ax, ay, az, bx, by, bz, shift, 4);
       }
@@ -224,25 +259,20 @@ __global__ void __launch_bounds__(WARPS * 32, 1) ragged_stream_kernel(const Ragg
     pending += QPL;
 
     __syncwarp();
-    if (pc.u < uend) {
-      if (lane == 0) {
-        fence_proxy_async_smem();
-        ragged_issue<CQ>(pc, stages + slot * STAGE_BYTES, &bars[slot]);
-      }
-      next_unit(pc);
+    if (pc.u < pc.uend) {
+      rc_issue<CQ, WARPS>(pc, p, lane, stages + slot * STAGE_BYTES, &metas[slot], &bars[slot]);
       ++issued;
     }
     slot = (slot + 1 == NSTAGE) ? 0 : slot + 1;
 
-    const int64_t unit = cc.u;
-    const bool unit_end = next_unit(cc);
+    const bool unit_end = (m.flags & 2) != 0;
     if (pending >= 4 || unit_end) {
 #pragma unroll
       for (int j = 0; j < NV; ++j) { cf_add(acc2[j], acc1[j]); acc1[j] = 0.f; }
       pending = 0;
     }
     if (unit_end) {
-      double* rec = p.sums + unit * SUMS_STRIDE;
+      double* rec = p.sums + m.rec * SUMS_STRIDE;
       CF v[16];
 #pragma unroll
       for (int j = 0; j < 16; ++j) v[j] = (j < NV) ? acc2[j < NV ? j : 0] : cf_zero();
@@ -361,7 +391,9 @@ struct RCfg {
 constexpr int kNumRCfg = 5;
 constexpr RCfg kRCfgs[kNumRCfg] = {{16, 128, 2}, {16, 64, 4}, {16, 64, 3}, {8, 128, 4}, {8, 64, 4}};
 
-size_t rcfg_smem(const RCfg& c) { return (size_t)c.warps * c.nstage * c.cq * 48 + (size_t)c.warps * c.nstage * 8; }
+size_t rcfg_smem(const RCfg& c) {
+  return (size_t)c.warps * c.nstage * c.cq * 48 + (size_t)c.warps * c.nstage * (8 + sizeof(ChunkMeta));
+}
 
 template <int CQ, int NS, int W>
 int launch_ragged_t(const RaggedArgs& a, int grid, cudaStream_t st) {
