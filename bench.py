@@ -48,6 +48,8 @@ WORKLOADS = {
     "allpairs_20000x2000": (20_000, 2_000, 50, 0.1, 5.0, 0.99),
     # ragged batch: (segments, atoms lo, atoms hi, frames lo, frames hi, sigma)
     "ragged_512": (512, 50, 20_000, 100, 5_000, 0.05),
+    # serving: (database frames, atoms, offered rates (requests/s), max query frames, slice lengths)
+    "serving_500000x300": (500_000, 300, (100, 300, 1000, 3000, 10000), 256, (10_000, 500_000)),
 }
 DEFAULT_WORKLOAD = "single_reference_200000x10000"
 
@@ -751,6 +753,205 @@ def run_reference(args) -> dict:
     }
 
 
+# ---------------------------------------------------------------------------
+# Serving workload
+# ---------------------------------------------------------------------------
+
+
+def serving_requests(db_host_frames, frame_ids, n, rate, seed, max_q, slice_range, n_db):
+    """n requests: query frames log-uniform in [1, max_q]; half against the
+    full database, half against a contiguous slice of uniform length in
+    slice_range; Poisson arrivals at `rate` per second.  Queries are database
+    frames (host copies in db_host_frames, indexed through frame_ids) plus
+    0.05 nm noise, a random rotation and a translation."""
+    from mdtraj_gb300 import serving, synth
+
+    rng = np.random.default_rng(seed)
+    reqs, t = [], 0.0
+    lo, hi = slice_range[0], min(slice_range[1], n_db)
+    for k in range(n):
+        Q = int(np.clip(np.floor(synth.log_uniform(rng, 1, max_q + 1, 1)[0]), 1, max_q))
+        if rng.random() < 0.5:
+            a, b = 0, n_db
+        else:
+            ln = int(rng.integers(min(lo, n_db), hi + 1))
+            a = int(rng.integers(0, n_db - ln + 1))
+            b = a + ln
+        pick = rng.integers(0, len(frame_ids), Q)
+        q = synth.perturbed_queries(db_host_frames, pick, seed=int(rng.integers(1 << 30)))
+        t += rng.exponential(1.0 / rate)
+        reqs.append(serving.Request(queries=q, db0=a, db1=b, arrival=t, rid=k))
+    return reqs
+
+
+def run_serving(args) -> dict:
+    """A 500,000-frame x 300-atom database resident in HBM (Gaussian-chain
+    backbones) answering Poisson streams of query sets (1-256 frames each,
+    full database or a slice) at offered rates from 100 to 10,000 requests/s.
+    Continuous batching over split-BF16 tensor-core cross tiles is compared
+    with one request per launch on the plain FP32 CUDA-core tiles, on the
+    same requests and the same GPU.  Latency = arrival to results in host
+    memory."""
+    import torch
+
+    from mdtraj_gb300 import _lib, cross, serving, synth
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    F, A, rates, max_q, slice_range = WORKLOADS[args.workload]
+    if args.frames:
+        F = args.frames
+    t_setup = time.perf_counter()
+    db_x = synth.gaussian_chain(F, A, seed=2024 + rank, device=dev)
+    dbs = cross.FrameSet.from_frames(db_x, device=dev)
+    frame_ids = np.random.default_rng(99).integers(0, F, 4096)
+    host_frames = db_x[torch.from_numpy(frame_ids).to(dev)].cpu().numpy()
+    del db_x
+    torch.cuda.empty_cache()
+    setup_s = time.perf_counter() - t_setup
+    lib = _lib.lib
+    server = serving.RmsdServer(dbs, method="tensor", query_capacity=16384, hbm_budget_bytes=48 << 30, slots=3)
+    base = serving.RmsdServer(dbs, method="fp32", query_capacity=1024, hbm_budget_bytes=48 << 30, slots=1,
+                              max_batch_requests=1)
+    warm = serving_requests(host_frames, frame_ids, 24, 1e6, 1, max_q, slice_range, F)
+    server.serve(warm, realtime=False, keep_results=False)
+    base.serve(serving_requests(host_frames, frame_ids, 4, 1e6, 2, max_q, slice_range, F), realtime=False,
+               keep_results=False)
+    sweep = []
+    with ClockSampler(local) as clk:
+        for k, rate in enumerate(rates):
+            n = max(20, min(int(rate * args.serve_seconds), args.serve_max))
+            reqs = serving_requests(host_frames, frame_ids, n, rate, 1000 + k, max_q, slice_range, F)
+            b0 = server.n_batches
+            done = server.serve(reqs, realtime=True, keep_results=False)
+            row = {"offered_rate": rate, "requests": n, "continuous": serving.latency_summary(done)}
+            row["continuous"]["mean_batch_requests"] = round(n / max(1, server.n_batches - b0), 2)
+            nb = min(n, args.baseline_max)
+            reqs_b = [serving.Request(queries=r.queries, db0=r.db0, db1=r.db1, arrival=r.arrival, rid=r.rid)
+                      for r in reqs[:nb]]
+            row["one_per_launch_fp32"] = serving.latency_summary(base.serve(reqs_b, realtime=True,
+                                                                             keep_results=False))
+            sweep.append(row)
+            print(json.dumps(row), file=sys.stderr, flush=True)
+    top = sweep[-1]
+    # kernel-level: one fixed batch (32 requests x 80 query frames, full database)
+    Qb, Rb = 80, 32
+    qset = cross.FrameSet(Qb * Rb, A, dev)
+    qx = torch.from_numpy(synth.perturbed_queries(host_frames, np.arange(Qb * Rb) % len(frame_ids), seed=5)
+                          .reshape(Qb * Rb, -1)).to(dev)
+    qset.prepare(qx, 0)
+    outb = torch.empty((Rb, Qb, F), dtype=torch.float32, device=dev)
+    table = cross.request_table([(outb[r].data_ptr(), r * Qb, Qb, 0, F) for r in range(Rb)])
+    wsb = cross.CrossWorkspace(dev).get(F, Qb * Rb, Rb)
+    stream = torch.cuda.current_stream().cuda_stream
+
+    def kernel_ms(method, reps):
+        cross.cross_launch(dbs, F, qset, table, Rb, method, wsb, stream)
+        torch.cuda.synchronize()
+        lib.gbrmsd_profile_enable(reps)
+        for _ in range(reps):
+            cross.cross_launch(dbs, F, qset, table, Rb, method, wsb, stream)
+        torch.cuda.synchronize()
+        kk = np.zeros(reps, dtype=np.float32)
+        nn = lib.gbrmsd_profile_read(kk.ctypes.data, reps)
+        lib.gbrmsd_profile_enable(0)
+        return float(np.mean(kk[:nn]))
+
+    k_tc = kernel_ms("tensor", 3)
+    got_tc = outb.cpu().numpy()
+    k_fp = kernel_ms("fp32", 1)
+    pairs_b = float(Qb * Rb) * F
+    p = ROOT / "MEASURED_PEAKS.json"
+    bf16_peak = json.loads(p.read_text())["bf16_tflops"] if p.exists() else 1900.0
+    alg = 3 * 18.0 * A * pairs_b
+    ach = alg / (k_tc / 1e3) / 1e12
+    roof = {"bound": "tensor", "achieved": round(ach, 1), "peak": bf16_peak, "unit": "TFLOP/s",
+            "frac": round(ach / bf16_peak, 4), "traffic": traffic_from_profiles("cross_tc_kernel", args.workload),
+            "kernel": "allpairs_tc_kernel<cross>", "kernel_ms": round(k_tc, 4), "algorithmic_flops_per_launch": alg,
+            "launch": "%d requests x %d query frames vs %d database frames" % (Rb, Qb, F),
+            "peak_src": "measured" if p.exists() else "fallback"}
+    # accuracy: sampled entries of the fixed batch against the FP64 oracle
+    from oracle import fp64
+
+    rng = np.random.default_rng(7)
+    qh = qx.view(Qb * Rb, A, 3).cpu().numpy()
+    errs = []
+    for _ in range(40):
+        qi = int(rng.integers(Qb * Rb))
+        cols = rng.integers(0, F, 50)
+        dbf = dbs_frames(dbs, cols, A)
+        want = fp64.kabsch_rmsd(dbf, qh[qi])
+        errs.append(np.abs(got_tc[qi // Qb, qi % Qb, cols] - want))
+    e = np.concatenate(errs)
+    cpu_base = None
+    if rank == 0 and world == 1 and not args.skip_cpu:
+        cpu_base = serving_cpu(dbs, F, A, qh[0], args.cpu_budget, top)
+    h2d = float(np.mean([r.queries.nbytes for r in reqs]))
+    d2h = float(np.mean([r.result_bytes for r in reqs]))
+    return {
+        "metric": "serving_queries_per_s", "value": top["continuous"]["queries_per_s"], "unit": "queries/s",
+        "n_gpus": world, "steps": len(rates), "warmup": 1,
+        "ms_per_step": round(1e3 / max(top["continuous"]["queries_per_s"], 1e-9), 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "bf16x3 (split hi/lo, f32 accumulate)",
+        "data": "synthetic (seeded Gaussian-chain database generated on device; perturbed database frames as queries)",
+        "config": {"workload": args.workload, "db_frames": F, "n_atoms": A, "offered_rates": list(rates),
+                   "query_frames": "log-uniform 1-%d" % max_q, "db_range": "full (50%%) or slice %d-%d" % slice_range,
+                   "slots": len(server.slots), "query_capacity": server.qcap, "setup_s": round(setup_s, 1),
+                   "latency": "arrival to results in pinned host memory",
+                   "l2": "database (%.1f GB prepared) larger than L2; no flush" % (dbs.buf.numel() / 1e9)},
+        "sweep": sweep,
+        "speedup_at_top_rate": round(top["continuous"]["queries_per_s"] /
+                                     max(1e-9, top["one_per_launch_fp32"]["queries_per_s"]), 2),
+        "roofline": roof,
+        "kernel_compare": {"tensor_ms": round(k_tc, 3), "fp32_ms": round(k_fp, 3),
+                           "tensor_vs_fp32": round(k_fp / k_tc, 2), "pairs": pairs_b},
+        "accuracy": {"checked_pairs": int(e.size), "max_err_nm": float(e.max()),
+                     "rms_err_nm": float(np.sqrt((e ** 2).mean())), "oracle": "FP64 Kabsch/SVD (oracle/fp64.py)"},
+        "cpu_baseline": cpu_base,
+        "e2e": {"value": top["continuous"]["queries_per_s"], "unit": "queries/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "note": "per request: query frames in, RMSD rows out"},
+        "gpu_launches": int(server.n_batches * 3),
+        "clocks": clk.summary(),
+    }
+
+
+def dbs_frames(dbs, idx, A):
+    """Centred float32 database frames idx (F_idx, A, 3) from a FrameSet."""
+    import torch
+
+    kpad = (A + 63) // 64 * 64
+    x32 = dbs.buf[:3 * dbs.capacity * kpad * 4].view(torch.float32).view(dbs.capacity, 3, kpad)
+    sel = x32[torch.from_numpy(np.asarray(idx)).to(x32.device)][:, :, :A]
+    return sel.transpose(1, 2).contiguous().cpu().numpy()
+
+
+def serving_cpu(dbs, F, A, q, budget_s, top) -> dict:
+    """The reference's per-query-frame md.rmsd over database frames, on the
+    host cores: frames/s on a bounded sample, converted to requests/s at the
+    sweep's mean pairs per request."""
+    from oracle import cpu
+
+    impl = cpu.best_available()
+    n = min(F, 100_000)
+    target = np.ascontiguousarray(dbs_frames(dbs, np.arange(n), A))
+    ref = np.ascontiguousarray(q)
+    t0 = time.perf_counter()
+    reps = 0
+    while True:
+        impl.md_rmsd(target.copy(), ref.copy())
+        reps += 1
+        if time.perf_counter() - t0 > budget_s or reps >= 50:
+            break
+    dt = time.perf_counter() - t0
+    pairs_s = reps * n / dt
+    mean_pairs = top["continuous"]["pairs_per_s"] / max(top["continuous"]["queries_per_s"], 1e-9)
+    return {"value": round(pairs_s / mean_pairs, 3), "unit": "queries/s", "cores": cpu.n_threads(),
+            "kind": impl.kind, "pairs_per_s": round(pairs_s, 1),
+            "sample": "%d x md.rmsd(%d database frames, 1 query frame) in %.1f s; queries/s at the sweep's mean "
+                      "pairs per request" % (reps, n, dt)}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -764,6 +965,9 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU baseline work")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--serve-seconds", type=float, default=2.0, help="offered load per rate (seconds of arrivals)")
+    ap.add_argument("--serve-max", type=int, default=1500, help="max requests per rate")
+    ap.add_argument("--baseline-max", type=int, default=300, help="max requests per rate for the one-per-launch baseline")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -772,6 +976,8 @@ def main():
         res = run_allpairs(args)
     elif args.workload.startswith("ragged"):
         res = run_ragged(args)
+    elif args.workload.startswith("serving"):
+        res = run_serving(args)
     else:
         res = run_gpu(args)
     rank = int(os.environ.get("RANK", "0"))

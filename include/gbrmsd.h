@@ -134,6 +134,42 @@ int gbrmsd_allpairs(const float* x, int64_t n_frames, int32_t n_atoms, int32_t n
  * this workspace refined exactly and whether a device error was recorded. */
 int gbrmsd_allpairs_status(const void* ws, int32_t* refined_pairs, void* stream);
 
+/* ---- Cross RMSD: query frames against a resident database ------------------
+ * Replaces `[md.rmsd(db[a:b], queries, k, precentered=True) for k in ...]`
+ * (_rmsd.pyx:64-243 per query frame) for many requests at once.  A frame set
+ * is a device buffer of prepared frames: centred float rows, split BF16 planes
+ * and FP64 traces, laid out for `capacity` frames of n_atoms atoms, filled by
+ * gbrmsd_frameset_prepare (rows [first, first + n_frames), any number of calls;
+ * centre as in gbrmsd_allpairs).
+ *
+ * gbrmsd_cross_rmsd scores, for every request r, its n_query frames (rows
+ * [pool0, pool0 + n_query) of the query set) against the database frames
+ * [db0, db1):  out_r[q * (db1 - db0) + (i - db0)] = rmsd(db frame i, query
+ * frame pool0 + q), float32, optimal superposition.  Requests may overlap in
+ * the database and share tiles (their query rows must not overlap); each
+ * result depends only on its own two frames.  method 0: FP32 CUDA-core tiles;
+ * method 1: split-BF16 tcgen05 tiles.  Near-identical pairs are recomputed
+ * exactly, as in gbrmsd_allpairs.  Errors and the refined-pair count are read
+ * with gbrmsd_allpairs_status(ws, ...).  No counterpart in the reference: it
+ * has no multi-reference call. */
+typedef struct gbrmsd_cross_request {
+  float* out;      /* device, n_query x (db1 - db0) float32 */
+  int64_t pool0;   /* first query-set row */
+  int64_t db0;     /* database frames [db0, db1) */
+  int64_t db1;
+  int32_t n_query;
+  int32_t reserved;
+} gbrmsd_cross_request_t;
+
+size_t gbrmsd_frameset_bytes(int64_t capacity, int32_t n_atoms);
+int gbrmsd_frameset_prepare(const float* x, int64_t n_frames, int32_t n_atoms, int32_t n_padded,
+                            int64_t frame_stride, int32_t layout, int32_t centre, void* set, int64_t capacity,
+                            int64_t first, void* stream);
+size_t gbrmsd_cross_workspace_bytes(int64_t n_db, int64_t query_capacity, int32_t n_requests);
+int gbrmsd_cross_rmsd(const void* db_set, int64_t db_capacity, int64_t n_db, const void* query_set,
+                      int64_t query_capacity, int32_t n_atoms, const gbrmsd_cross_request_t* requests,
+                      int32_t n_requests, int32_t method, void* ws, size_t ws_bytes, void* stream);
+
 /* ---- Ragged batch: many trajectories in one launch -------------------------
  * Each segment s is a trajectory of seg_frames[s] frames of seg_atoms[s] atoms
  * (padded to seg_padded[s], a multiple of 4), atom-major, starting at float

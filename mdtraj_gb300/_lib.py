@@ -52,6 +52,10 @@ SIGNATURES: dict[str, tuple] = {
     "gbrmsd_allpairs_workspace_bytes": (_sz, [_i64, _i32]),
     "gbrmsd_allpairs": (C.c_int, [_vp, _i64, _i32, _i32, _i64, _i32, _i32, _i32, _vp, _vp, _sz, _vp]),
     "gbrmsd_allpairs_status": (C.c_int, [_vp, _vp, _vp]),
+    "gbrmsd_frameset_bytes": (_sz, [_i64, _i32]),
+    "gbrmsd_frameset_prepare": (C.c_int, [_vp, _i64, _i32, _i32, _i64, _i32, _i32, _vp, _i64, _i64, _vp]),
+    "gbrmsd_cross_workspace_bytes": (_sz, [_i64, _i64, _i32]),
+    "gbrmsd_cross_rmsd": (C.c_int, [_vp, _i64, _i64, _vp, _i64, _i32, _vp, _i32, _i32, _vp, _sz, _vp]),
     "gbrmsd_ragged_config_count": (C.c_int, []),
     "gbrmsd_ragged_plan": (C.c_int, [_vp, _vp, _vp, _vp, _i32, _i32, _i32, _vp]),
     "gbrmsd_ragged_setup": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
@@ -69,6 +73,13 @@ SIGNATURES: dict[str, tuple] = {
     "gbrmsd_copy_rows_kernel": (C.c_int, [_vp, _i64, _vp, _i64, _i64, _i64, _i64, _vp]),
     "gbrmsd_write_centred": (C.c_int, [_vp, _vp, _i64, _vp, _i64, _i32, _vp]),
 }
+
+
+class CrossRequest(C.Structure):
+    """gbrmsd_cross_request_t (include/gbrmsd.h)."""
+
+    _fields_ = [("out", C.c_void_p), ("pool0", C.c_int64), ("db0", C.c_int64), ("db1", C.c_int64),
+                ("n_query", C.c_int32), ("reserved", C.c_int32)]
 
 
 class RaggedPlan(C.Structure):

@@ -18,6 +18,9 @@
 #include <math.h>
 #include <string.h>
 
+#include <algorithm>
+#include <vector>
+
 #include "allpairs.cuh"
 #include "capi_internal.h"
 #include "common.cuh"
@@ -118,18 +121,47 @@ __device__ __forceinline__ void tri_tile(int64_t t, int64_t nb, int64_t& bi, int
   bj = r + (t - start(r));
 }
 
-__global__ void __launch_bounds__(256, 1) allpairs_fp32_kernel(const float* __restrict__ X32,
-                                                               const double* __restrict__ G, int64_t F, int32_t A,
-                                                               int32_t kpad, int64_t nb, float* __restrict__ out,
-                                                               PairRefine* rl, int* rc, int rcap, int* err) {
+// Arguments of the FP32 tile kernel.  All-pairs: X32b == X32, one upper-
+// triangle tile per CTA.  Cross: rows from a database set, columns from a
+// query set, tiles from a list.
+struct Fp32Args {
+  const float* X32;   // row frames
+  const double* G;
+  int64_t F;          // row frames
+  const float* X32b;  // column frames
+  const double* Gb;
+  int64_t Fb;         // column frames (capacity of the query set)
+  int32_t A, kpad;
+  int64_t nb;         // all-pairs: frame blocks per side
+  float* out;         // all-pairs output
+  const int2* tiles;  // cross: (row block, column block)
+  const gbrmsd_cross_request_t* reqs;
+  const int32_t* colreq;
+  PairRefine* rl;
+  int* rc;
+  int rcap;
+  int* err;
+};
+
+template <bool CROSS>
+__global__ void __launch_bounds__(256, 1) allpairs_fp32_kernel(const Fp32Args p) {
   extern __shared__ __align__(16) float sm[];
   float* sA = sm;                                  // [2][TROWS][LDS_STRIDE]
   float* sB = sm + 2 * TROWS * LDS_STRIDE;         // [2][TROWS][LDS_STRIDE]
   int64_t bi, bj;
-  tri_tile(blockIdx.x, nb, bi, bj);
+  if (CROSS) {
+    const int2 t = p.tiles[blockIdx.x];
+    bi = t.x;
+    bj = t.y;
+  } else {
+    tri_tile(blockIdx.x, p.nb, bi, bj);
+  }
+  const float* __restrict__ X32 = p.X32;
+  const float* __restrict__ X32b = p.X32b;
+  const int32_t kpad = p.kpad;
   const int tid = threadIdx.x;
   const int ty = tid >> 4, tx = tid & 15;
-  const int64_t rowsA = bi * TROWS, rowsB = bj * TROWS, nrows = 3 * F;
+  const int64_t rowsA = bi * TROWS, rowsB = bj * TROWS, nrows = 3 * p.F, nrowsb = 3 * p.Fb;
 
   auto load_block = [&](int buf, int kb) {
     for (int idx = tid; idx < TROWS * (KB / 4); idx += 256) {
@@ -138,8 +170,8 @@ __global__ void __launch_bounds__(256, 1) allpairs_fp32_kernel(const float* __re
       const size_t col = (size_t)kb * KB + 4 * c4;
       cp_async16(&sA[(buf * TROWS + r) * LDS_STRIDE + 4 * c4], X32 + (ga < nrows ? (size_t)ga * kpad + col : 0),
                  ga < nrows);
-      cp_async16(&sB[(buf * TROWS + r) * LDS_STRIDE + 4 * c4], X32 + (gbr < nrows ? (size_t)gbr * kpad + col : 0),
-                 gbr < nrows);
+      cp_async16(&sB[(buf * TROWS + r) * LDS_STRIDE + 4 * c4], X32b + (gbr < nrowsb ? (size_t)gbr * kpad + col : 0),
+                 gbr < nrowsb);
     }
     cp_async_commit();
   };
@@ -189,24 +221,48 @@ __global__ void __launch_bounds__(256, 1) allpairs_fp32_kernel(const float* __re
     __syncthreads();
   }
 
-  const float inv_n = 1.0f / (float)A;
-#pragma unroll
-  for (int fa = 0; fa < 3; ++fa)
+  const float inv_n = 1.0f / (float)p.A;
+  if (CROSS) {
 #pragma unroll
     for (int fb = 0; fb < 3; ++fb) {
-      const int64_t i = bi * TBF + ty * 3 + fa, j = bj * TBF + tx * 3 + fb;
-      if (i < F && j < F && i <= j) pair_epilogue(i, j, acc[fa][fb], G, inv_n, F, out, rl, rc, rcap, err);
+      const int64_t j = bj * TBF + tx * 3 + fb;
+      const CrossCol cv = cross_col(p.reqs, p.colreq, j, p.Fb);
+      if (cv.row == nullptr) continue;
+#pragma unroll
+      for (int fa = 0; fa < 3; ++fa) {
+        const int64_t i = bi * TBF + ty * 3 + fa;
+        if (i >= cv.db0 && i < cv.db1 && i < p.F)
+          cross_pair(i, j, acc[fa][fb], (float)p.G[i], (float)p.Gb[j], inv_n, cv.row + (i - cv.db0), p.rl, p.rc,
+                     p.rcap, p.err);
+      }
     }
+  } else {
+#pragma unroll
+    for (int fa = 0; fa < 3; ++fa)
+#pragma unroll
+      for (int fb = 0; fb < 3; ++fb) {
+        const int64_t i = bi * TBF + ty * 3 + fa, j = bj * TBF + tx * 3 + fb;
+        if (i < p.F && j < p.F && i <= j)
+          pair_epilogue(i, j, acc[fa][fb], p.G, inv_n, p.F, p.out, p.rl, p.rc, p.rcap, p.err);
+      }
+  }
 }
 
 // ---------------------------------------------------------------------------
 // Refinement of near-identical pairs (warp per pair)
 // ---------------------------------------------------------------------------
 
+// Cross: i indexes X32/G (database), j indexes X32b/Gb (query set) and the
+// result goes to the request's output row; all-pairs: X32b == X32.
+template <bool CROSS>
 __global__ void __launch_bounds__(256) allpairs_refine_kernel(const float* __restrict__ X32,
                                                               const double* __restrict__ G, int64_t F, int32_t A,
                                                               int32_t kpad, const PairRefine* rl, const int* rc,
-                                                              int rcap, float* __restrict__ out) {
+                                                              int rcap, float* __restrict__ out,
+                                                              const float* __restrict__ X32b,
+                                                              const double* __restrict__ Gb, int64_t Fb,
+                                                              const gbrmsd_cross_request_t* reqs,
+                                                              const int32_t* colreq) {
   const int lane = threadIdx.x & 31;
   const int64_t W = (int64_t)gridDim.x * (blockDim.x >> 5);
   int n = *reinterpret_cast<const volatile int*>(rc);
@@ -214,7 +270,8 @@ __global__ void __launch_bounds__(256) allpairs_refine_kernel(const float* __res
   for (int64_t e = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); e < n; e += W) {
     const int64_t i = rl[e].i, j = rl[e].j;
     const float* ai[3] = {X32 + (size_t)(3 * i) * kpad, X32 + (size_t)(3 * i + 1) * kpad, X32 + (size_t)(3 * i + 2) * kpad};
-    const float* bj[3] = {X32 + (size_t)(3 * j) * kpad, X32 + (size_t)(3 * j + 1) * kpad, X32 + (size_t)(3 * j + 2) * kpad};
+    const float* bj[3] = {X32b + (size_t)(3 * j) * kpad, X32b + (size_t)(3 * j + 1) * kpad,
+                          X32b + (size_t)(3 * j + 2) * kpad};
     // compensated 3x3 inner product
     CF v[16];
 #pragma unroll
@@ -244,7 +301,7 @@ __global__ void __launch_bounds__(256) allpairs_refine_kernel(const float* __res
       const float lo = __shfl_sync(FULL_MASK, v[0].lo, 2 * t);
       m[t] = (double)hi + (double)lo;
     }
-    const double ga = G[i], gb = G[j];
+    const double ga = G[i], gb = Gb[j];
     int iters = 0;
     const double lam = qcp_lambda_max(m, ga, gb, &iters);
     double rot[9];
@@ -279,8 +336,13 @@ __global__ void __launch_bounds__(256) allpairs_refine_kernel(const float* __res
       double msd = cf_to_double(acc) / (double)A;
       if (!(msd > 0.0)) msd = 0.0;
       const float r = (float)sqrt(msd);
-      out[i * F + j] = r;
-      out[j * F + i] = r;
+      if (CROSS) {
+        const CrossCol cv = cross_col(reqs, colreq, j, Fb);
+        if (cv.row != nullptr) cv.row[i - cv.db0] = r;
+      } else {
+        out[i * F + j] = r;
+        out[j * F + i] = r;
+      }
     }
   }
 }
@@ -310,6 +372,102 @@ ApWs ap_ws(int64_t F, int32_t A) {
 // Implemented in allpairs_tc.cu: split-BF16 tcgen05 tiles.
 int launch_allpairs_tc(const __nv_bfloat16* Xhi, const __nv_bfloat16* Xlo, const double* G, int64_t F, int32_t A,
                        int32_t kpad, float* out, PairRefine* rl, int* rc, int rcap, int* err, cudaStream_t st);
+int launch_cross_tc(const __nv_bfloat16* Ahi, const __nv_bfloat16* Alo, const double* Ga, int64_t n_a, int64_t cap_a,
+                    const __nv_bfloat16* Bhi, const __nv_bfloat16* Blo, const double* Gb, int64_t cap_b, int32_t A,
+                    int32_t kpad, const gbrmsd_cross_request_t* reqs, const int32_t* colreq, const int2* tiles,
+                    int64_t n_tiles, PairRefine* rl, int* rc, int rcap, int* err, cudaStream_t st);
+int cross_tc_block_frames(int* rows, int* cols);
+
+namespace {
+
+// Frame set: [X32 (3 cap x kpad floats) | hi | lo (BF16) | G (cap doubles)].
+struct FsLayout {
+  size_t x32, hi, lo, g, total;
+  int32_t kpad;
+};
+
+FsLayout fs_layout(int64_t cap, int32_t A) {
+  FsLayout l;
+  l.kpad = (A + 63) / 64 * 64;
+  const size_t rows = (size_t)3 * (size_t)cap;
+  l.x32 = 0;
+  l.hi = align_up(rows * l.kpad * 4, 256);
+  l.lo = align_up(l.hi + rows * l.kpad * 2, 256);
+  l.g = align_up(l.lo + rows * l.kpad * 2, 256);
+  l.total = align_up(l.g + (size_t)cap * 8, 256);
+  return l;
+}
+
+// Cross workspace: [header | requests | column -> request | tiles | refinement list].
+struct CrossWs {
+  size_t reqs, colreq, tiles, rl, total;
+  int64_t max_tiles;
+  int rcap;
+};
+
+int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+CrossWs cross_ws(int64_t n_db, int64_t qcap, int32_t n_req) {
+  int fm = 1, fn = 1;
+  cross_tc_block_frames(&fm, &fn);
+  CrossWs w;
+  w.max_tiles = std::max(ceil_div(n_db, fm) * ceil_div(qcap, fn), ceil_div(n_db, TBF) * ceil_div(qcap, TBF));
+  w.reqs = 256;
+  w.colreq = align_up(w.reqs + (size_t)n_req * sizeof(gbrmsd_cross_request_t), 256);
+  w.tiles = align_up(w.colreq + (size_t)qcap * sizeof(int32_t), 256);
+  w.rl = align_up(w.tiles + (size_t)w.max_tiles * sizeof(int2), 256);
+  const int64_t pairs = n_db * qcap;
+  w.rcap = (int)(pairs < (1 << 22) ? (pairs > 0 ? pairs : 1) : (1 << 22));
+  w.total = align_up(w.rl + (size_t)w.rcap * sizeof(PairRefine), 256);
+  return w;
+}
+
+// Validates the requests, fills the column -> request map and lists the
+// (row block, column block) tiles that hold at least one requested pair:
+// per column block, the row blocks between the lowest and highest database
+// frame its requests ask for; row-block-major so that CTAs running at the same
+// time share database rows in L2.
+int build_cross_tiles(const gbrmsd_cross_request_t* reqs, int32_t n_req, int64_t n_db, int64_t qcap, int fr_rows,
+                      int fr_cols, std::vector<int2>& tiles, std::vector<int32_t>& colreq) {
+  colreq.assign((size_t)qcap, -1);
+  const int64_t ncb = ceil_div(qcap, fr_cols);
+  std::vector<int64_t> lo((size_t)ncb, INT64_MAX), hi((size_t)ncb, -1);
+  for (int32_t r = 0; r < n_req; ++r) {
+    const gbrmsd_cross_request_t& q = reqs[r];
+    if (q.n_query < 0 || q.pool0 < 0 || q.pool0 + q.n_query > qcap || q.db0 < 0 || q.db1 < q.db0 || q.db1 > n_db)
+      return set_error(GBRMSD_E_INVALID,
+                       "cross: request %d needs 0 <= pool0, pool0 + n_query <= query capacity and "
+                       "0 <= db0 <= db1 <= n_db",
+                       r);
+    if (q.n_query == 0 || q.db1 == q.db0) continue;
+    if (!q.out) return set_error(GBRMSD_E_INVALID, "cross: request %d has no output buffer", r);
+    for (int64_t j = q.pool0; j < q.pool0 + q.n_query; ++j) {
+      if (colreq[(size_t)j] >= 0) return set_error(GBRMSD_E_INVALID, "cross: requests %d and %d share query row %lld",
+                                                   colreq[(size_t)j], r, (long long)j);
+      colreq[(size_t)j] = r;
+    }
+    const int64_t rb0 = q.db0 / fr_rows, rb1 = (q.db1 - 1) / fr_rows;
+    for (int64_t cb = q.pool0 / fr_cols; cb <= (q.pool0 + q.n_query - 1) / fr_cols; ++cb) {
+      lo[(size_t)cb] = std::min(lo[(size_t)cb], rb0);
+      hi[(size_t)cb] = std::max(hi[(size_t)cb], rb1);
+    }
+  }
+  std::vector<int32_t> active;
+  int64_t rmin = INT64_MAX, rmax = -1;
+  for (int64_t cb = 0; cb < ncb; ++cb)
+    if (hi[(size_t)cb] >= 0) {
+      active.push_back((int32_t)cb);
+      rmin = std::min(rmin, lo[(size_t)cb]);
+      rmax = std::max(rmax, hi[(size_t)cb]);
+    }
+  tiles.clear();
+  for (int64_t rb = rmin; rb <= rmax; ++rb)
+    for (int32_t cb : active)
+      if (rb >= lo[(size_t)cb] && rb <= hi[(size_t)cb]) tiles.push_back(make_int2((int)rb, cb));
+  return GBRMSD_OK;
+}
+
+}  // namespace
 
 }  // namespace gb
 
@@ -370,11 +528,27 @@ int gbrmsd_allpairs(const float* x, int64_t n_frames, int32_t n_atoms, int32_t n
     const int64_t nb = (n_frames + TBF - 1) / TBF;
     const int64_t tiles = nb * (nb + 1) / 2;
     if (tiles > 0x7fffffffLL) return set_error(GBRMSD_E_INVALID, "allpairs: too many tiles");
-    GB_CUDA_TRY(cudaFuncSetAttribute(allpairs_fp32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, FP32_TILE_SMEM),
+    GB_CUDA_TRY(cudaFuncSetAttribute(allpairs_fp32_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     FP32_TILE_SMEM),
                 "cudaFuncSetAttribute(allpairs_fp32_kernel)");
+    Fp32Args fa;
+    memset(&fa, 0, sizeof(fa));
+    fa.X32 = X32;
+    fa.G = G;
+    fa.F = n_frames;
+    fa.X32b = X32;
+    fa.Gb = G;
+    fa.Fb = n_frames;
+    fa.A = n_atoms;
+    fa.kpad = kpad;
+    fa.nb = nb;
+    fa.out = out;
+    fa.rl = rl;
+    fa.rc = hdr + 1;
+    fa.rcap = L.rcap;
+    fa.err = hdr;
     prof_begin(st);
-    allpairs_fp32_kernel<<<(unsigned)tiles, 256, FP32_TILE_SMEM, st>>>(X32, G, n_frames, n_atoms, kpad, nb, out, rl,
-                                                                       hdr + 1, L.rcap, hdr);
+    allpairs_fp32_kernel<false><<<(unsigned)tiles, 256, FP32_TILE_SMEM, st>>>(fa);
     GB_CUDA_TRY(cudaGetLastError(), "launch allpairs_fp32_kernel");
     prof_end(st);
   } else {
@@ -383,8 +557,127 @@ int gbrmsd_allpairs(const float* x, int64_t n_frames, int32_t n_atoms, int32_t n
     if (rc) return rc;
     prof_end(st);
   }
-  allpairs_refine_kernel<<<sm_count() * 4, 256, 0, st>>>(X32, G, n_frames, n_atoms, kpad, rl, hdr + 1, L.rcap, out);
+  allpairs_refine_kernel<false><<<sm_count() * 4, 256, 0, st>>>(X32, G, n_frames, n_atoms, kpad, rl, hdr + 1, L.rcap,
+                                                                 out, X32, G, n_frames, nullptr, nullptr);
   GB_CUDA_TRY(cudaGetLastError(), "launch allpairs_refine_kernel");
+  return GBRMSD_OK;
+}
+
+size_t gbrmsd_frameset_bytes(int64_t capacity, int32_t n_atoms) {
+  if (capacity < 0 || n_atoms < 1) return 0;
+  return fs_layout(capacity, n_atoms).total;
+}
+
+int gbrmsd_frameset_prepare(const float* x, int64_t n_frames, int32_t n_atoms, int32_t n_padded,
+                            int64_t frame_stride, int32_t layout, int32_t centre, void* set, int64_t capacity,
+                            int64_t first, void* stream) {
+  clear_error();
+  if (n_frames < 0 || n_atoms < 1 || first < 0 || first + n_frames > capacity)
+    return set_error(GBRMSD_E_INVALID, "frameset_prepare: need n_atoms >= 1 and 0 <= first <= first + n_frames <= capacity");
+  if (layout != ATOM_MAJOR && layout != AXIS_MAJOR) return set_error(GBRMSD_E_INVALID, "frameset_prepare: bad layout");
+  if (n_padded < n_atoms || frame_stride < 3LL * n_padded)
+    return set_error(GBRMSD_E_INVALID, "frameset_prepare: n_padded / frame_stride too small");
+  if (capacity > (1LL << 31) / 3) return set_error(GBRMSD_E_INVALID, "frameset_prepare: capacity too large");
+  if (n_frames == 0) return GBRMSD_OK;
+  if (!x || !set || !aligned16(set)) return set_error(GBRMSD_E_INVALID, "frameset_prepare: null or misaligned pointer");
+  const FsLayout L = fs_layout(capacity, n_atoms);
+  unsigned char* b = static_cast<unsigned char*>(set);
+  const size_t row0 = (size_t)3 * (size_t)first * L.kpad;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int64_t blocks = std::min<int64_t>((int64_t)sm_count() * 8, (n_frames + 7) / 8);
+  allpairs_prep_kernel<<<(unsigned)blocks, 256, 0, st>>>(
+      x, n_frames, n_atoms, n_padded, frame_stride, layout, centre ? 1 : 0, L.kpad,
+      reinterpret_cast<float*>(b + L.x32) + row0, reinterpret_cast<__nv_bfloat16*>(b + L.hi) + row0,
+      reinterpret_cast<__nv_bfloat16*>(b + L.lo) + row0, reinterpret_cast<double*>(b + L.g) + first);
+  GB_CUDA_TRY(cudaGetLastError(), "launch frameset prep kernel");
+  return GBRMSD_OK;
+}
+
+size_t gbrmsd_cross_workspace_bytes(int64_t n_db, int64_t query_capacity, int32_t n_requests) {
+  if (n_db < 0 || query_capacity < 0 || n_requests < 0) return 0;
+  return cross_ws(n_db, query_capacity, n_requests).total;
+}
+
+int gbrmsd_cross_rmsd(const void* db_set, int64_t db_capacity, int64_t n_db, const void* query_set,
+                      int64_t query_capacity, int32_t n_atoms, const gbrmsd_cross_request_t* requests,
+                      int32_t n_requests, int32_t method, void* ws, size_t ws_bytes, void* stream) {
+  clear_error();
+  if (n_atoms < 1 || n_db < 0 || n_db > db_capacity || query_capacity < 0 || n_requests < 0)
+    return set_error(GBRMSD_E_INVALID, "cross: need n_atoms >= 1, 0 <= n_db <= db_capacity, query_capacity >= 0");
+  if (db_capacity > (1LL << 31) / 3 || query_capacity > (1LL << 31) / 3)
+    return set_error(GBRMSD_E_INVALID, "cross: set capacity too large");
+  if (method != 0 && method != 1) return set_error(GBRMSD_E_INVALID, "cross: method must be 0 (fp32) or 1 (tensor)");
+  if (n_requests > 0 && !requests) return set_error(GBRMSD_E_INVALID, "cross: null request table");
+  if (!db_set || !query_set || !aligned16(db_set) || !aligned16(query_set))
+    return set_error(GBRMSD_E_INVALID, "cross: null or misaligned frame set");
+  const CrossWs W = cross_ws(n_db, query_capacity, n_requests);
+  if (!ws || ws_bytes < W.total || !aligned16(ws))
+    return set_error(GBRMSD_E_WORKSPACE, "cross: workspace needs %zu bytes", W.total);
+  int fm = TBF, fn = TBF;
+  if (method == 1) cross_tc_block_frames(&fm, &fn);
+  std::vector<int2> tiles;
+  std::vector<int32_t> colreq;
+  int rc = build_cross_tiles(requests, n_requests, n_db, query_capacity, fm, fn, tiles, colreq);
+  if (rc) return rc;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  unsigned char* w = static_cast<unsigned char*>(ws);
+  int* hdr = reinterpret_cast<int*>(w);
+  GB_CUDA_TRY(cudaMemsetAsync(hdr, 0, 8, st), "memset cross header");
+  if (tiles.empty()) return GBRMSD_OK;
+  auto* dreq = reinterpret_cast<gbrmsd_cross_request_t*>(w + W.reqs);
+  auto* dcol = reinterpret_cast<int32_t*>(w + W.colreq);
+  auto* dtiles = reinterpret_cast<int2*>(w + W.tiles);
+  auto* rl = reinterpret_cast<PairRefine*>(w + W.rl);
+  GB_CUDA_TRY(cudaMemcpyAsync(dreq, requests, sizeof(gbrmsd_cross_request_t) * n_requests, cudaMemcpyHostToDevice, st),
+              "upload cross requests");
+  GB_CUDA_TRY(cudaMemcpyAsync(dcol, colreq.data(), sizeof(int32_t) * colreq.size(), cudaMemcpyHostToDevice, st),
+              "upload column map");
+  GB_CUDA_TRY(cudaMemcpyAsync(dtiles, tiles.data(), sizeof(int2) * tiles.size(), cudaMemcpyHostToDevice, st),
+              "upload cross tiles");
+  const FsLayout La = fs_layout(db_capacity, n_atoms), Lb = fs_layout(query_capacity, n_atoms);
+  const unsigned char* a = static_cast<const unsigned char*>(db_set);
+  const unsigned char* b = static_cast<const unsigned char*>(query_set);
+  const float* X32a = reinterpret_cast<const float*>(a + La.x32);
+  const float* X32b = reinterpret_cast<const float*>(b + Lb.x32);
+  const double* Ga = reinterpret_cast<const double*>(a + La.g);
+  const double* Gb = reinterpret_cast<const double*>(b + Lb.g);
+  if (method == 0) {
+    GB_CUDA_TRY(cudaFuncSetAttribute(allpairs_fp32_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     FP32_TILE_SMEM),
+                "cudaFuncSetAttribute(cross_fp32_kernel)");
+    Fp32Args fa;
+    memset(&fa, 0, sizeof(fa));
+    fa.X32 = X32a;
+    fa.G = Ga;
+    fa.F = n_db;
+    fa.X32b = X32b;
+    fa.Gb = Gb;
+    fa.Fb = query_capacity;
+    fa.A = n_atoms;
+    fa.kpad = La.kpad;
+    fa.tiles = dtiles;
+    fa.reqs = dreq;
+    fa.colreq = dcol;
+    fa.rl = rl;
+    fa.rc = hdr + 1;
+    fa.rcap = W.rcap;
+    fa.err = hdr;
+    prof_begin(st);
+    allpairs_fp32_kernel<true><<<(unsigned)tiles.size(), 256, FP32_TILE_SMEM, st>>>(fa);
+    GB_CUDA_TRY(cudaGetLastError(), "launch cross_fp32_kernel");
+    prof_end(st);
+  } else {
+    prof_begin(st);
+    rc = launch_cross_tc(reinterpret_cast<const __nv_bfloat16*>(a + La.hi), reinterpret_cast<const __nv_bfloat16*>(a + La.lo),
+                         Ga, n_db, db_capacity, reinterpret_cast<const __nv_bfloat16*>(b + Lb.hi),
+                         reinterpret_cast<const __nv_bfloat16*>(b + Lb.lo), Gb, query_capacity, n_atoms, La.kpad, dreq,
+                         dcol, dtiles, (int64_t)tiles.size(), rl, hdr + 1, W.rcap, hdr, st);
+    if (rc) return rc;
+    prof_end(st);
+  }
+  allpairs_refine_kernel<true><<<sm_count() * 4, 256, 0, st>>>(X32a, Ga, n_db, n_atoms, La.kpad, rl, hdr + 1, W.rcap,
+                                                                nullptr, X32b, Gb, query_capacity, dreq, dcol);
+  GB_CUDA_TRY(cudaGetLastError(), "launch cross refine kernel");
   return GBRMSD_OK;
 }
 

@@ -11,6 +11,7 @@
 
 #include <stdint.h>
 
+#include "../../include/gbrmsd.h"
 #include "common.cuh"
 
 namespace gb {
@@ -67,6 +68,57 @@ __device__ __forceinline__ float qcp_msd_f32(const float (&m)[9], float ga, floa
     x -= step;
     if (!(fabsf(step) > 2e-7f)) break;
   }
+  // The quartic's largest root is ill-conditioned when the top eigenvalues of
+  // K are close (far-apart structures): FP32 Newton stalls ~1e-6 away from it.
+  // The eigenvalue itself is well-conditioned, so polish x with the Rayleigh
+  // quotient of v = the row of adj(K - x I) with the largest diagonal
+  // cofactor (parallel to the top eigenvector; the quotient's error is
+  // quadratic in v's): x += v^T (K - x I) v / v^T v.  The adjugate comes from
+  // the 2x2 complementary minors of rows {0,1} and {2,3} (Laplace expansion).
+  {
+    const float b00 = k00 - x, b11 = k11 - x, b22 = k22 - x, b33 = k33 - x;
+    const float b01 = k01, b02 = k02, b03 = k03, b12 = k12, b13 = k13, b23 = k23;
+    const float u0 = b00 * b11 - b01 * b01, u1 = b00 * b12 - b01 * b02, u2 = b00 * b13 - b01 * b03;
+    const float u3 = b01 * b12 - b11 * b02, u4 = b01 * b13 - b11 * b03, u5 = b02 * b13 - b12 * b03;
+    const float w5 = b22 * b33 - b23 * b23, w4 = b12 * b33 - b13 * b23, w3 = b12 * b23 - b13 * b22;
+    const float w2 = b02 * b33 - b03 * b23, w1 = b02 * b23 - b03 * b22, w0 = b02 * b13 - b03 * b12;
+    const float a00 = b11 * w5 - b12 * w4 + b13 * w3;
+    const float a11 = b00 * w5 - b02 * w2 + b03 * w1;
+    const float a22 = b03 * u4 - b13 * u2 + b33 * u0;
+    const float a33 = b02 * u3 - b12 * u1 + b22 * u0;
+    float v0, v1, v2, v3, best = fabsf(a00);
+    v0 = a00;
+    v1 = -b01 * w5 + b02 * w4 - b03 * w3;
+    v2 = b13 * u5 - b23 * u4 + b33 * u3;
+    v3 = -b12 * u5 + b22 * u4 - b23 * u3;
+    if (fabsf(a11) > best) {
+      best = fabsf(a11);
+      v0 = -b01 * w5 + b12 * w2 - b13 * w1;
+      v1 = a11;
+      v2 = -b03 * u5 + b23 * u2 - b33 * u1;
+      v3 = b02 * u5 - b22 * u2 + b23 * u1;
+    }
+    if (fabsf(a22) > best) {
+      best = fabsf(a22);
+      v0 = b01 * w4 - b11 * w2 + b13 * w0;
+      v1 = -b00 * w4 + b01 * w2 - b03 * w0;
+      v2 = a22;
+      v3 = -b02 * u4 + b12 * u2 - b23 * u0;
+    }
+    if (fabsf(a33) > best) {
+      v0 = -b01 * w3 + b11 * w1 - b12 * w0;
+      v1 = b00 * w3 - b01 * w1 + b02 * w0;
+      v2 = -b03 * u3 + b13 * u1 - b23 * u0;
+      v3 = a33;
+    }
+    const float bv0 = b00 * v0 + b01 * v1 + b02 * v2 + b03 * v3;
+    const float bv1 = b01 * v0 + b11 * v1 + b12 * v2 + b13 * v3;
+    const float bv2 = b02 * v0 + b12 * v1 + b22 * v2 + b23 * v3;
+    const float bv3 = b03 * v0 + b13 * v1 + b23 * v2 + b33 * v3;
+    const float vv = v0 * v0 + v1 * v1 + v2 * v2 + v3 * v3;
+    const float dx = (v0 * bv0 + v1 * bv1 + v2 * bv2 + v3 * bv3) / vv;
+    if (vv > 1e-30f && fabsf(dx) < 1e-3f) x += dx;
+  }
   const float msd = 2.0f * lam0 * (1.0f - x) * inv_n;
   return msd > 0.f ? msd : 0.f;
 }
@@ -88,6 +140,49 @@ __device__ __forceinline__ void pair_epilogue(int64_t i, int64_t j, const float 
   const float r = sqrtf(msd);
   out[i * F + j] = r;
   out[j * F + i] = r;
+  const float scale = 0.5f * (ga + gb) * inv_n;
+  if (r < 0.25f * scale * sqrtf(inv_n)) {
+    const int slot = atomicAdd(rc, 1);
+    if (slot < rcap)
+      rl[slot] = PairRefine{(int32_t)i, (int32_t)j};
+    else
+      atomicOr(err, DEV_ERR_REFINE_OVERFLOW);
+  }
+}
+
+// Cross RMSD (query set against a database): the output row and database
+// range of one query-set column, or row == nullptr when the column belongs to
+// no request of the call.
+struct CrossCol {
+  float* row;  // out_r + q * (db1 - db0)
+  int64_t db0, db1;
+};
+
+__device__ __forceinline__ CrossCol cross_col(const gbrmsd_cross_request_t* __restrict__ reqs,
+                                              const int32_t* __restrict__ colreq, int64_t j, int64_t n_cols) {
+  CrossCol c;
+  c.row = nullptr;
+  c.db0 = 0;
+  c.db1 = 0;
+  if (j < n_cols) {
+    const int32_t r = colreq[j];
+    if (r >= 0) {
+      const gbrmsd_cross_request_t q = reqs[r];
+      c.row = q.out + (j - q.pool0) * (q.db1 - q.db0);
+      c.db0 = q.db0;
+      c.db1 = q.db1;
+    }
+  }
+  return c;
+}
+
+// Cross pair (database frame i, query row j): FP32 QCP, result to *dst, and
+// the same refinement rule as pair_epilogue.
+__device__ __forceinline__ void cross_pair(int64_t i, int64_t j, const float (&m)[9], float ga, float gb,
+                                           float inv_n, float* dst, PairRefine* rl, int* rc, int rcap, int* err) {
+  const float msd = qcp_msd_f32(m, ga, gb, inv_n);
+  const float r = sqrtf(msd);
+  *dst = r;
   const float scale = 0.5f * (ga + gb) * inv_n;
   if (r < 0.25f * scale * sqrtf(inv_n)) {
     const int slot = atomicAdd(rc, 1);

@@ -61,24 +61,30 @@ constexpr int NEPI_THREADS = 32 * NEPI;
 constexpr int NTHREADS = 64 + NEPI_THREADS;
 constexpr uint32_t SPIN = 1u << 24;
 
-// smem: [stages | epilogue staging | barriers | tmem address]
+// smem: [stages | epilogue staging | barriers | tmem address | cross column views]
 constexpr int SMEM_STAGES = NSTAGE * STAGE_BYTES;
 constexpr int SMEM_EPI = SMEM_STAGES;
 constexpr int SMEM_BAR = SMEM_EPI + ((EPI_BYTES + 127) / 128) * 128;
-constexpr int SMEM_TOTAL = SMEM_BAR + 128 + 1024;  // + slack for 1024-byte alignment
+constexpr int SMEM_COLV = SMEM_BAR + 128;
+constexpr int SMEM_TOTAL = SMEM_COLV + FR_N * (int)sizeof(CrossCol) + 1024;  // + slack for 1024-byte alignment
 
 struct TcArgs {
-  const double* G;
+  const double* G;    // traces of the row frames
   const int2* tiles;  // (row block, column block)
   int64_t n_tiles;
-  int64_t F;
+  int64_t F;          // row frames (all-pairs: also the column frames)
   int32_t A;
   int32_t kpad;
-  float* out;
+  float* out;         // all-pairs output (F x F)
   PairRefine* rl;
   int* rc;
   int rcap;
   int* err;
+  // cross RMSD only: column frames come from a query set
+  const double* Gb;
+  const gbrmsd_cross_request_t* reqs;
+  const int32_t* colreq;
+  int64_t n_b;
 };
 
 // ---- PTX wrappers ----------------------------------------------------------
@@ -163,6 +169,7 @@ __device__ __forceinline__ bool wait_bar(uint64_t* bar, uint32_t parity, int* er
   return mbar_wait_bounded(bar, parity, err, SPIN);
 }
 
+template <bool CROSS>
 __global__ void __launch_bounds__(NTHREADS, 1) allpairs_tc_kernel(const __grid_constant__ CUtensorMap map_hi_a,
                                                                   const __grid_constant__ CUtensorMap map_lo_a,
                                                                   const __grid_constant__ CUtensorMap map_hi_b,
@@ -179,6 +186,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) allpairs_tc_kernel(const __grid_c
   uint64_t* kempty = kfull + 2;           // [2] k-block buffer folded by all accumulator warps
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(kempty + 2);
   volatile int* fail_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+  CrossCol* colv = reinterpret_cast<CrossCol*>(smem + SMEM_COLV);
 
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
@@ -301,10 +309,11 @@ __global__ void __launch_bounds__(NTHREADS, 1) allpairs_tc_kernel(const __grid_c
       // the whole tile is in registers: stage it 48 columns (16 frames) at a time
       named_bar(1, NEPI_THREADS);
       const bool proceed = *fail_flag == 0;
-      named_bar(1, NEPI_THREADS);
-      if (!proceed) break;
       const int2 tl = args.tiles[t];
       const int64_t i0 = (int64_t)tl.x * FR_M, j0 = (int64_t)tl.y * FR_N;
+      if (CROSS && etid < FR_N) colv[etid] = cross_col(args.reqs, args.colreq, j0 + etid, args.n_b);
+      named_bar(1, NEPI_THREADS);
+      if (!proceed) break;
       for (int ch = 0; ch < TILE_N / EPI_COLS; ++ch) {
         const int lo = ch * EPI_COLS - grp * GCOLS;  // my column q maps to staging column q - lo
         float* dst = sD + row * EPI_LD;
@@ -314,16 +323,36 @@ __global__ void __launch_bounds__(NTHREADS, 1) allpairs_tc_kernel(const __grid_c
           if (c >= 0 && c < EPI_COLS) dst[c] = acc[q];
         }
         named_bar(1, NEPI_THREADS);
-        for (int p = etid; p < FR_M * 16; p += NEPI_THREADS) {
-          const int li = p >> 4, lj = p & 15;
-          const int64_t i = i0 + li, j = j0 + ch * 16 + lj;
-          if (i < args.F && j < args.F && i <= j) {
-            float m[9];
+        if (CROSS) {
+          // consecutive threads take consecutive database frames of one query
+          // column: contiguous in the request's output row
+          for (int p = etid; p < FR_M * 16; p += NEPI_THREADS) {
+            const int lj = p / FR_M, li = p - lj * FR_M;
+            const int64_t i = i0 + li;
+            const CrossCol cv = colv[ch * 16 + lj];
+            if (cv.row != nullptr && i >= cv.db0 && i < cv.db1 && i < args.F) {
+              float m[9];
 #pragma unroll
-            for (int c = 0; c < 3; ++c)
+              for (int c = 0; c < 3; ++c)
 #pragma unroll
-              for (int d = 0; d < 3; ++d) m[3 * c + d] = sD[(3 * li + c) * EPI_LD + 3 * lj + d];
-            pair_epilogue(i, j, m, args.G, inv_n, args.F, args.out, args.rl, args.rc, args.rcap, args.err);
+                for (int d = 0; d < 3; ++d) m[3 * c + d] = sD[(3 * li + c) * EPI_LD + 3 * lj + d];
+              const int64_t j = j0 + ch * 16 + lj;
+              cross_pair(i, j, m, (float)args.G[i], (float)args.Gb[j], inv_n, cv.row + (i - cv.db0), args.rl,
+                         args.rc, args.rcap, args.err);
+            }
+          }
+        } else {
+          for (int p = etid; p < FR_M * 16; p += NEPI_THREADS) {
+            const int li = p >> 4, lj = p & 15;
+            const int64_t i = i0 + li, j = j0 + ch * 16 + lj;
+            if (i < args.F && j < args.F && i <= j) {
+              float m[9];
+#pragma unroll
+              for (int c = 0; c < 3; ++c)
+#pragma unroll
+                for (int d = 0; d < 3; ++d) m[3 * c + d] = sD[(3 * li + c) * EPI_LD + 3 * lj + d];
+              pair_epilogue(i, j, m, args.G, inv_n, args.F, args.out, args.rl, args.rc, args.rcap, args.err);
+            }
           }
         }
         named_bar(1, NEPI_THREADS);
@@ -415,13 +444,64 @@ int launch_allpairs_tc(const __nv_bfloat16* Xhi, const __nv_bfloat16* Xlo, const
   a.rc = rc;
   a.rcap = rcap;
   a.err = err;
-  GB_CUDA_TRY(cudaFuncSetAttribute(allpairs_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_TOTAL),
+  a.Gb = nullptr;
+  a.reqs = nullptr;
+  a.colreq = nullptr;
+  a.n_b = 0;
+  GB_CUDA_TRY(cudaFuncSetAttribute(allpairs_tc_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_TOTAL),
               "cudaFuncSetAttribute(allpairs_tc_kernel)");
   const int64_t grid = a.n_tiles < sm_count() ? a.n_tiles : sm_count();
-  allpairs_tc_kernel<<<(unsigned)grid, NTHREADS, SMEM_TOTAL, st>>>(mha, mla, mhb, mlb, a);
+  allpairs_tc_kernel<false><<<(unsigned)grid, NTHREADS, SMEM_TOTAL, st>>>(mha, mla, mhb, mlb, a);
   GB_CUDA_TRY(cudaGetLastError(), "launch allpairs_tc_kernel");
   // (a pageable host->device cudaMemcpyAsync returns once the source has been
   // staged, so the host tile list may go out of scope here)
+  return GBRMSD_OK;
+}
+
+int launch_cross_tc(const __nv_bfloat16* Ahi, const __nv_bfloat16* Alo, const double* Ga, int64_t n_a, int64_t cap_a,
+                    const __nv_bfloat16* Bhi, const __nv_bfloat16* Blo, const double* Gb, int64_t cap_b, int32_t A,
+                    int32_t kpad, const gbrmsd_cross_request_t* reqs, const int32_t* colreq, const int2* tiles,
+                    int64_t n_tiles, PairRefine* rl, int* rc, int rcap, int* err, cudaStream_t st) {
+  if (kpad % KBLK) return set_error(GBRMSD_E_INVALID, "cross_tc: k padding must be a multiple of 64");
+  if (max_dyn_smem() < SMEM_TOTAL) return set_error(GBRMSD_E_UNSUPPORTED, "cross_tc: not enough shared memory");
+  if (n_tiles == 0) return GBRMSD_OK;
+  alignas(64) CUtensorMap mha, mla, mhb, mlb;
+  memset(&mha, 0, sizeof(mha));
+  memset(&mla, 0, sizeof(mla));
+  memset(&mhb, 0, sizeof(mhb));
+  memset(&mlb, 0, sizeof(mlb));
+  int rc0 = encode_plane(&mha, Ahi, 3 * cap_a, kpad, TILE_M);
+  if (!rc0) rc0 = encode_plane(&mla, Alo, 3 * cap_a, kpad, TILE_M);
+  if (!rc0) rc0 = encode_plane(&mhb, Bhi, 3 * cap_b, kpad, TILE_N);
+  if (!rc0) rc0 = encode_plane(&mlb, Blo, 3 * cap_b, kpad, TILE_N);
+  if (rc0) return rc0;
+  TcArgs a;
+  a.G = Ga;
+  a.tiles = tiles;
+  a.n_tiles = n_tiles;
+  a.F = n_a;
+  a.A = A;
+  a.kpad = kpad;
+  a.out = nullptr;
+  a.rl = rl;
+  a.rc = rc;
+  a.rcap = rcap;
+  a.err = err;
+  a.Gb = Gb;
+  a.reqs = reqs;
+  a.colreq = colreq;
+  a.n_b = cap_b;
+  GB_CUDA_TRY(cudaFuncSetAttribute(allpairs_tc_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_TOTAL),
+              "cudaFuncSetAttribute(cross_tc_kernel)");
+  const int64_t grid = n_tiles < sm_count() ? n_tiles : sm_count();
+  allpairs_tc_kernel<true><<<(unsigned)grid, NTHREADS, SMEM_TOTAL, st>>>(mha, mla, mhb, mlb, a);
+  GB_CUDA_TRY(cudaGetLastError(), "launch cross_tc_kernel");
+  return GBRMSD_OK;
+}
+
+int cross_tc_block_frames(int* rows, int* cols) {
+  *rows = FR_M;
+  *cols = FR_N;
   return GBRMSD_OK;
 }
 

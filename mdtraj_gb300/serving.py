@@ -1,0 +1,261 @@
+"""Serving loop: a database of frames resident in HBM answering RMSD query
+sets with continuous batching.
+
+A request is a set of query frames scored against a contiguous range of the
+database (``[md.rmsd(db[a:b], queries, k) for k]``, see cross.py).  The
+server keeps the prepared database on the device and runs a host loop that
+
+  * moves requests whose arrival time has passed into a FIFO queue;
+  * admits queued requests while the query pool (prepared query frames on the
+    device) has room for their frames and the HBM budget has room for their
+    results;
+  * whenever one of its stream slots is free, launches every admitted request
+    as ONE batch on that slot: query upload, preparation into the pool, one
+    cross-RMSD launch whose tiles mix the requests, and the copy of each
+    result to pinned host memory;
+  * completes batches whose events have fired, releasing pool rows and budget.
+
+So requests that arrive while others are on the GPU join the next batch as
+soon as a slot and memory free up, batches on different slots overlap on the
+device (one batch's kernel with another's copies), and batches grow with the
+load.  A request's results depend only on its own frames: the same alone and
+in any mix.  ``slots=1, max_batch_requests=1`` gives one request per launch.
+"""
+from __future__ import annotations
+
+import math
+import time
+from collections import deque
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _device as D
+from .cross import CrossWorkspace, FrameSet, cross_launch, cross_status, request_table
+
+
+@dataclass
+class Request:
+    """Query frames (Q, A, 3) float32 against database frames [db0, db1)."""
+
+    queries: np.ndarray
+    db0: int
+    db1: int
+    arrival: float = 0.0  # seconds after the start of serve()
+    rid: int = -1
+    result: np.ndarray | None = None  # (Q, db1 - db0) float32 once done
+    t_admit: float = math.nan
+    t_launch: float = math.nan
+    t_done: float = math.nan
+    batch: int = -1
+    refined: int = 0
+    _p0: int = field(default=-1, repr=False)
+    _out: torch.Tensor | None = field(default=None, repr=False)
+    _host: torch.Tensor | None = field(default=None, repr=False)
+
+    @property
+    def n_query(self) -> int:
+        return int(self.queries.shape[0])
+
+    @property
+    def result_bytes(self) -> int:
+        return 4 * self.n_query * (self.db1 - self.db0)
+
+    @property
+    def latency(self) -> float:
+        return self.t_done - self.arrival
+
+
+class PoolAllocator:
+    """First-fit allocator of contiguous query-pool rows."""
+
+    def __init__(self, capacity: int):
+        self.capacity = int(capacity)
+        self.free = [(0, self.capacity)]  # sorted, disjoint (start, length)
+
+    def alloc(self, n: int):
+        for k, (s, ln) in enumerate(self.free):
+            if ln >= n:
+                if ln == n:
+                    del self.free[k]
+                else:
+                    self.free[k] = (s + n, ln - n)
+                return s
+        return None
+
+    def release(self, start: int, n: int) -> None:
+        self.free.append((start, n))
+        self.free.sort()
+        merged = []
+        for s, ln in self.free:
+            if merged and merged[-1][0] + merged[-1][1] == s:
+                merged[-1] = (merged[-1][0], merged[-1][1] + ln)
+            else:
+                merged.append((s, ln))
+        self.free = merged
+
+    @property
+    def free_rows(self) -> int:
+        return sum(ln for _, ln in self.free)
+
+
+class _Slot:
+    def __init__(self, device):
+        self.stream = torch.cuda.Stream(device=device)
+        self.ws = CrossWorkspace(device)
+        self.event = None
+        self.batch = None
+        self.ws_buf = None
+
+
+class RmsdServer:
+    """Resident database + continuous-batching request loop.
+
+    database: FrameSet, or frames (host array / device tensor (F, A, 3)).
+    method: "tensor" (split-BF16 tcgen05 tiles) or "fp32" (CUDA-core tiles).
+    query_capacity: frames in the device query pool.
+    hbm_budget_bytes: device bytes for results of admitted requests.
+    slots: batches that may be in flight at once (one stream each).
+    max_batch_requests: cap on requests per batch (None: no cap).
+    result_to_host: copy each result to pinned host memory (else results stay
+    on the device as tensors).
+    """
+
+    def __init__(self, database, *, method: str = "tensor", query_capacity: int = 8192,
+                 hbm_budget_bytes: int = 8 << 30, slots: int = 3, max_batch_requests: int | None = None,
+                 result_to_host: bool = True, device=None):
+        self.device = device if device is not None else D.require_device()
+        self.db = database if isinstance(database, FrameSet) else FrameSet.from_frames(database, device=self.device)
+        self.n_db = self.db.capacity
+        self.n_atoms = self.db.n_atoms
+        self.method = method
+        self.qcap = int(query_capacity)
+        self.qset = FrameSet(self.qcap, self.n_atoms, self.device)
+        self.staging = torch.empty((self.qcap, 3 * self.n_atoms), dtype=torch.float32, device=self.device)
+        self.pool = PoolAllocator(self.qcap)
+        self.budget = int(hbm_budget_bytes)
+        self.used = 0
+        self.slots = [_Slot(self.device) for _ in range(max(1, int(slots)))]
+        self.max_batch = max_batch_requests
+        self.result_to_host = result_to_host
+        self.n_batches = 0
+        self.batch_sizes = []
+
+    # -- request checks ---------------------------------------------------
+    def validate(self, r: Request) -> None:
+        q = r.queries
+        if q.ndim != 3 or q.shape[1] != self.n_atoms or q.shape[2] != 3 or q.dtype != np.float32:
+            raise ValueError(f"request {r.rid}: queries must be float32 (Q, {self.n_atoms}, 3)")
+        if not (1 <= q.shape[0] <= self.qcap):
+            raise ValueError(f"request {r.rid}: 1 <= n_query <= query capacity ({self.qcap})")
+        if not (0 <= r.db0 < r.db1 <= self.n_db):
+            raise ValueError(f"request {r.rid}: database range must satisfy 0 <= db0 < db1 <= {self.n_db}")
+        if r.result_bytes > self.budget:
+            raise ValueError(f"request {r.rid}: result ({r.result_bytes} bytes) exceeds the HBM budget")
+
+    # -- steps of the loop ----------------------------------------------------
+    def _admit(self, r: Request, now: float) -> bool:
+        if self.used + r.result_bytes > self.budget:
+            return False
+        p0 = self.pool.alloc(r.n_query)
+        if p0 is None:
+            return False
+        r._p0 = p0
+        r._out = torch.empty(r.n_query * (r.db1 - r.db0), dtype=torch.float32, device=self.device)
+        self.used += r.result_bytes
+        r.t_admit = now
+        return True
+
+    def _launch(self, slot: _Slot, batch: list, now: float) -> None:
+        s = slot.stream
+        with torch.cuda.stream(s):
+            for r in batch:
+                rows = self.staging[r._p0:r._p0 + r.n_query]
+                rows.copy_(torch.from_numpy(r.queries.reshape(r.n_query, -1)), non_blocking=True)
+                self.qset.prepare(rows, r._p0, stream=s.cuda_stream)
+            table = request_table([(r._out.data_ptr(), r._p0, r.n_query, r.db0, r.db1) for r in batch])
+            ws = slot.ws.get(self.n_db, self.qcap, len(batch))
+            cross_launch(self.db, self.n_db, self.qset, table, len(batch), self.method, ws, s.cuda_stream)
+            if self.result_to_host:
+                for r in batch:
+                    r._host = torch.empty(r._out.numel(), dtype=torch.float32, pin_memory=True)
+                    r._host.copy_(r._out, non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record(s)
+        for r in batch:
+            r.t_launch = now
+            r.batch = self.n_batches
+        self.n_batches += 1
+        self.batch_sizes.append(len(batch))
+        slot.event, slot.batch, slot.ws_buf = ev, batch, ws
+
+    def _complete(self, slot: _Slot, now: float, keep_results: bool) -> list:
+        refined = cross_status(slot.ws_buf, slot.stream.cuda_stream)  # raises on a device error
+        done = slot.batch
+        for r in done:
+            shape = (r.n_query, r.db1 - r.db0)
+            if keep_results:
+                r.result = (r._host.numpy() if self.result_to_host else r._out).reshape(shape)
+            r.refined = refined
+            r.t_done = now
+            self.pool.release(r._p0, r.n_query)
+            self.used -= r.result_bytes
+            r._out = None if self.result_to_host or not keep_results else r._out
+            if not keep_results:
+                r._host = None
+        slot.event, slot.batch, slot.ws_buf = None, None, None
+        return done
+
+    # -- the loop ------------------------------------------------------------
+    def serve(self, requests, *, realtime: bool = True, keep_results: bool = True, poll_s: float = 50e-6) -> list:
+        """Runs the loop over `requests` (arrival times in seconds from the
+        start; realtime=False queues everything at once and resets the
+        arrival times to 0).  Returns the requests with results and timings,
+        in completion order."""
+        reqs = sorted(requests, key=lambda r: r.arrival)
+        for r in reqs:
+            self.validate(r)
+            if not realtime:
+                r.arrival = 0.0
+        n = len(reqs)
+        queue, admitted, finished = deque(), [], []
+        nxt = 0
+        t0 = time.perf_counter()
+        while len(finished) < n:
+            now = time.perf_counter() - t0
+            while nxt < n and (not realtime or reqs[nxt].arrival <= now):
+                queue.append(reqs[nxt])
+                nxt += 1
+            for slot in self.slots:
+                if slot.event is not None and slot.event.query():
+                    finished.extend(self._complete(slot, time.perf_counter() - t0, keep_results))
+            while queue and (self.max_batch is None or len(admitted) < self.max_batch):
+                if not self._admit(queue[0], now):
+                    break
+                admitted.append(queue.popleft())
+            free = [s for s in self.slots if s.event is None]
+            if admitted and free:
+                self._launch(free[0], admitted, now)
+                admitted = []
+                continue
+            busy = any(s.event is not None for s in self.slots)
+            if not busy and not admitted and not queue and nxt < n:
+                wait = reqs[nxt].arrival - (time.perf_counter() - t0)
+                if wait > 0:
+                    time.sleep(min(wait, 0.01) if wait > 2e-3 else 0)
+            elif busy:
+                time.sleep(poll_s if poll_s > 0 else 0)
+        return finished
+
+
+def latency_summary(done: list, t_first: float | None = None) -> dict:
+    """p50 / p99 / mean latency (ms) and completed queries per second."""
+    lat = np.array([r.latency for r in done]) * 1e3
+    t0 = min(r.arrival for r in done) if t_first is None else t_first
+    t1 = max(r.t_done for r in done)
+    return {"requests": len(done), "p50_ms": round(float(np.percentile(lat, 50)), 3),
+            "p99_ms": round(float(np.percentile(lat, 99)), 3), "mean_ms": round(float(lat.mean()), 3),
+            "queries_per_s": round(len(done) / max(t1 - t0, 1e-9), 1),
+            "query_frames_per_s": round(sum(r.n_query for r in done) / max(t1 - t0, 1e-9), 1),
+            "pairs_per_s": round(sum(r.n_query * (r.db1 - r.db0) for r in done) / max(t1 - t0, 1e-9), 1)}

@@ -188,3 +188,54 @@ def ragged_shapes(n_seg: int = 512, seed: int = 0, atoms=(50, 20000), frames=(10
     a = np.rint(np.exp(rng.uniform(math.log(atoms[0]), math.log(atoms[1]), n_seg))).astype(np.int32)
     f = rng.integers(frames[0], frames[1] + 1, n_seg).astype(np.int64)
     return a, f
+
+
+def gaussian_chain(n_frames: int, n_atoms: int, seed: int = 0, device="cpu", bond: float = 0.38,
+                   angle_deg: float = 120.0, sigma: float = 0.05, chunk: int = 131072):
+    """Serving database frames: each frame is an independent backbone chain
+    of `n_atoms` beads with fixed bond length `bond` (nm) and bond angle
+    `angle_deg`, torsions uniform in [-pi, pi), plus i.i.d. N(0, sigma^2)
+    noise per coordinate.  Built bead by bead (each new bead placed from the
+    previous three), vectorised over frames.  Returns a float32 torch tensor
+    (F, A, 3) on `device`."""
+    import torch
+
+    g = torch.Generator(device=device)
+    g.manual_seed(int(seed))
+    out = torch.empty((n_frames, n_atoms, 3), dtype=torch.float32, device=device)
+    th = math.radians(angle_deg)
+    ct, st = math.cos(th), math.sin(th)
+    for s0 in range(0, n_frames, chunk):
+        n = min(chunk, n_frames - s0)
+        pos = torch.zeros((n, n_atoms, 3), dtype=torch.float32, device=device)
+        if n_atoms > 1:
+            pos[:, 1, 0] = bond
+        if n_atoms > 2:
+            pos[:, 2, 0] = bond - bond * ct
+            pos[:, 2, 1] = bond * st
+        tors = (torch.rand((n, n_atoms), generator=g, device=device) * 2 - 1) * math.pi
+        for k in range(3, n_atoms):
+            a, b, c = pos[:, k - 3], pos[:, k - 2], pos[:, k - 1]
+            bc = c - b
+            bc = bc / bc.norm(dim=1, keepdim=True)
+            nrm = torch.cross(b - a, bc, dim=1)
+            nrm = nrm / nrm.norm(dim=1, keepdim=True).clamp_min(1e-12)
+            m = torch.cross(nrm, bc, dim=1)
+            phi = tors[:, k:k + 1]
+            pos[:, k] = c + bond * (-ct * bc + st * torch.cos(phi) * m + st * torch.sin(phi) * nrm)
+        pos += torch.randn(pos.shape, generator=g, device=device) * sigma
+        out[s0:s0 + n] = pos
+    return out
+
+
+def perturbed_queries(db, idx, seed: int = 0, sigma: float = 0.05, translate: float = 2.0) -> np.ndarray:
+    """Query frames: database frames `idx` (host or device (F, A, 3)) plus
+    N(0, sigma^2) noise, a Haar-random rotation and a uniform translation in
+    [-translate, translate]^3.  Returns float32 numpy (len(idx), A, 3)."""
+    rng = np.random.default_rng(seed)
+    base = db[idx]
+    base = base.cpu().numpy() if hasattr(base, "cpu") else np.asarray(base)
+    base = base.astype(np.float64) + rng.normal(size=base.shape) * sigma
+    rot = haar_rotations(len(idx), rng)
+    t = rng.uniform(-translate, translate, size=(len(idx), 1, 3))
+    return np.ascontiguousarray(np.einsum("fkj,fij->fki", base, rot) + t, dtype=np.float32)

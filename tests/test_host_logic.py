@@ -146,3 +146,62 @@ def test_ragged_layout_is_padded_and_aligned():
     assert list(padded) == [8, 8, 4]
     assert list(off) == [0, 2 * 3 * 8, 2 * 3 * 8 + 3 * 3 * 8]
     assert all(o % 4 == 0 for o in off) and total == off[-1] + 4 * 3 * 4
+
+
+def test_pool_allocator_first_fit_and_merge():
+    from mdtraj_gb300.serving import PoolAllocator
+
+    p = PoolAllocator(100)
+    a, b, c = p.alloc(30), p.alloc(50), p.alloc(20)
+    assert (a, b, c) == (0, 30, 80) and p.alloc(1) is None
+    p.release(b, 50)
+    assert p.alloc(60) is None and p.alloc(40) == 30
+    p.release(a, 30)
+    p.release(30, 40)
+    p.release(c, 20)
+    assert p.free == [(0, 100)] and p.free_rows == 100
+
+
+def test_cross_request_validation_in_library():
+    """gbrmsd_cross_rmsd validates the request table before any device call."""
+    import ctypes as C
+
+    from mdtraj_gb300 import _lib
+    from mdtraj_gb300.cross import request_table
+
+    lib = _lib.lib
+    fake = 1 << 20  # 16-byte aligned stand-in pointers: never dereferenced on these paths
+    ws_bytes = lib.gbrmsd_cross_workspace_bytes(100, 16, 2)
+    assert lib.gbrmsd_cross_workspace_bytes(100, 16, 100) > ws_bytes >= lib.gbrmsd_cross_workspace_bytes(100, 16, 1) > 0
+
+    def call(reqs, method=1, n_db=100):
+        t = request_table(reqs)
+        return lib.gbrmsd_cross_rmsd(fake, 100, n_db, fake, 16, 8, C.addressof(t), len(reqs), method, fake, ws_bytes, None)
+
+    assert call([(fake, 0, 4, 0, 10), (fake, 3, 2, 0, 10)]) == _lib.E_INVALID
+    assert b"share query row" in lib.gbrmsd_last_error()
+    assert call([(fake, 14, 4, 0, 10)]) == _lib.E_INVALID          # beyond the query capacity
+    assert call([(fake, 0, 4, 5, 101)]) == _lib.E_INVALID          # beyond the database
+    assert call([(None, 0, 4, 0, 10)]) == _lib.E_INVALID           # no output
+    assert call([(fake, 0, 4, 0, 10)], method=2) == _lib.E_INVALID
+    assert call([(fake, 0, 4, 0, 10)], n_db=101) == _lib.E_INVALID  # more frames than the set holds
+    t = request_table([(fake, 0, 4, 0, 10)])
+    assert lib.gbrmsd_cross_rmsd(fake, 100, 100, fake, 16, 8, C.addressof(t), 1, 1, fake, ws_bytes - 1,
+                                 None) == _lib.E_WORKSPACE
+
+
+def test_gaussian_chain_geometry():
+    import math
+
+    from mdtraj_gb300 import synth
+
+    x = synth.gaussian_chain(3, 40, seed=2, sigma=0.0).double().numpy()
+    d = np.diff(x, axis=1)
+    np.testing.assert_allclose(np.linalg.norm(d, axis=2), 0.38, atol=1e-5)
+    u, v = d[:, :-1], d[:, 1:]
+    cosang = -(u * v).sum(2) / (np.linalg.norm(u, axis=2) * np.linalg.norm(v, axis=2))
+    np.testing.assert_allclose(cosang, math.cos(math.radians(120.0)), atol=1e-4)
+    q = synth.perturbed_queries(x.astype(np.float32), [1, 2], seed=0, sigma=0.0)
+    from oracle import fp64
+
+    assert fp64.kabsch_rmsd(q[:1], x[1])[0] < 1e-5
