@@ -169,6 +169,38 @@ __device__ __forceinline__ bool wait_bar(uint64_t* bar, uint32_t parity, int* er
   return mbar_wait_bounded(bar, parity, err, SPIN);
 }
 
+// Epilogue staging: accumulator column q of column group G goes to staging
+// column q - lo of chunk C (lo = 48 C - 80 G) when it falls inside the chunk.
+// One instantiation per (G, C) so that the column ranges are compile-time.
+template <int G, int C>
+__device__ __forceinline__ void stage_chunk_t(float* dst, const float (&acc)[GCOLS]) {
+  constexpr int lo = C * EPI_COLS - G * GCOLS;
+#pragma unroll
+  for (int q = 0; q < GCOLS; ++q)
+    if (q - lo >= 0 && q - lo < EPI_COLS) dst[q - lo] = acc[q];
+}
+
+__device__ __forceinline__ void stage_chunk(int gc, float* dst, const float (&acc)[GCOLS]) {
+  static_assert(NGROUP == 3 && TILE_N / EPI_COLS == 5, "staging cases");
+  switch (gc) {
+    case 0: stage_chunk_t<0, 0>(dst, acc); break;
+    case 1: stage_chunk_t<0, 1>(dst, acc); break;
+    case 2: stage_chunk_t<0, 2>(dst, acc); break;
+    case 3: stage_chunk_t<0, 3>(dst, acc); break;
+    case 4: stage_chunk_t<0, 4>(dst, acc); break;
+    case 5: stage_chunk_t<1, 0>(dst, acc); break;
+    case 6: stage_chunk_t<1, 1>(dst, acc); break;
+    case 7: stage_chunk_t<1, 2>(dst, acc); break;
+    case 8: stage_chunk_t<1, 3>(dst, acc); break;
+    case 9: stage_chunk_t<1, 4>(dst, acc); break;
+    case 10: stage_chunk_t<2, 0>(dst, acc); break;
+    case 11: stage_chunk_t<2, 1>(dst, acc); break;
+    case 12: stage_chunk_t<2, 2>(dst, acc); break;
+    case 13: stage_chunk_t<2, 3>(dst, acc); break;
+    default: stage_chunk_t<2, 4>(dst, acc); break;
+  }
+}
+
 template <bool CROSS>
 __global__ void __launch_bounds__(NTHREADS, 1) allpairs_tc_kernel(const __grid_constant__ CUtensorMap map_hi_a,
                                                                   const __grid_constant__ CUtensorMap map_lo_a,
@@ -315,13 +347,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) allpairs_tc_kernel(const __grid_c
       named_bar(1, NEPI_THREADS);
       if (!proceed) break;
       for (int ch = 0; ch < TILE_N / EPI_COLS; ++ch) {
-        const int lo = ch * EPI_COLS - grp * GCOLS;  // my column q maps to staging column q - lo
-        float* dst = sD + row * EPI_LD;
-#pragma unroll
-        for (int q = 0; q < GCOLS; ++q) {
-          const int c = q - lo;
-          if (c >= 0 && c < EPI_COLS) dst[c] = acc[q];
-        }
+        stage_chunk(grp * (TILE_N / EPI_COLS) + ch, sD + row * EPI_LD, acc);
         named_bar(1, NEPI_THREADS);
         if (CROSS) {
           // consecutive threads take consecutive database frames of one query
