@@ -134,6 +134,51 @@ int gbrmsd_allpairs(const float* x, int64_t n_frames, int32_t n_atoms, int32_t n
  * this workspace refined exactly and whether a device error was recorded. */
 int gbrmsd_allpairs_status(const void* ws, int32_t* refined_pairs, void* stream);
 
+/* ---- Superposition: rotations, in-place alignment, RMSF --------------------
+ * gbrmsd_rotations: the optimal rotation of every frame's alignment atoms onto
+ * a prepared reference -- the computeRot = 1 branch of msdFromMandG
+ * (src/theobald_rmsd.cpp:279-332) as driven by superpose_atom_major,
+ * rmsf and getMultipleAlignDisplaceRMSDs_atom_major (_rmsd.pyx:246-759).
+ * out_rot[9 f ..] is R, row-major, with R (a - mu_f) the frame aligned onto
+ * the reference (this equals the reference's own `rot` array for the
+ * frame-vs-reference call order of getMultipleAlignDisplaceRMSDs_atom_major).
+ * mode CENTER centres each frame on its own centroid (FP64, written to
+ * out_centroid if given); PRECENTERED uses the coordinates as given with the
+ * traces g_target / g_ref.  out_rmsd (optional) receives the RMSD as
+ * gbrmsd_rmsd_to_reference would.  ws: gbrmsd_rotations_workspace_bytes.
+ *
+ * gbrmsd_apply_rotations: in place, every atom of every frame (atom-major,
+ * frame_stride floats apart): x <- R_f (x - mu_f) + offset, where
+ * (x - mu_f) and (y + offset) are rounded to float as from FP64 (within one
+ * float ulp; Trajectory.superpose, core/trajectory.py:1127-1165, with
+ * rot_atom_major, src/rotation_generic.h:29-44).  centroids (n_frames x 3
+ * doubles, device) and offset3 (3 doubles, host) may be null (zero).  If
+ * nonzero0 (device int) is given it is set to 1 when any rotated coordinate of
+ * frame 0 is non-zero (the reference's overflow check,
+ * core/trajectory.py:1157-1163).
+ *
+ * gbrmsd_rmsf: per-atom root-mean-square fluctuation over the frames of x
+ * (atom-major), each frame first rotated about the origin by R_f when rot is
+ * given (rmsf, _rmsd.pyx:419-451: mean position per atom, then mean squared
+ * deviation).  ws: gbrmsd_rmsf_workspace_bytes.
+ *
+ * gbrmsd_rotated_rmsd: out[f] = sqrt(sum_k |R_f x_fk - ref_k|^2 / n_atoms)
+ * (rot_msd_atom_major, src/rotation_generic.h:47-103, as used by
+ * getMultipleAlignDisplaceRMSDs_atom_major); ref_frame is n_atoms x 3 floats.
+ */
+size_t gbrmsd_rotations_workspace_bytes(int64_t n_frames, int32_t n_atoms);
+int gbrmsd_rotations(const float* x, int64_t n_frames, int32_t n_atoms, int32_t n_padded, int64_t frame_stride,
+                     int32_t layout, int32_t mode, const void* ref_ws, const float* g_target, float g_ref,
+                     float* out_rot, double* out_centroid, float* out_rmsd, void* ws, size_t ws_bytes,
+                     void* stream);
+int gbrmsd_apply_rotations(float* x, int64_t n_frames, int32_t n_atoms, int64_t frame_stride, const float* rot,
+                           const double* centroids, const double* offset3, int32_t* nonzero0, void* stream);
+size_t gbrmsd_rmsf_workspace_bytes(int64_t n_frames, int32_t n_atoms);
+int gbrmsd_rmsf(const float* x, int64_t n_frames, int32_t n_atoms, int64_t frame_stride, const float* rot,
+                float* out_rmsf, void* ws, size_t ws_bytes, void* stream);
+int gbrmsd_rotated_rmsd(const float* x, int64_t n_frames, int32_t n_atoms, int64_t frame_stride, const float* rot,
+                        const float* ref_frame, float* out_rmsd, void* stream);
+
 /* ---- Cross RMSD: query frames against a resident database ------------------
  * Replaces `[md.rmsd(db[a:b], queries, k, precentered=True) for k in ...]`
  * (_rmsd.pyx:64-243 per query frame) for many requests at once.  A frame set

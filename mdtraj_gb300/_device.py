@@ -68,6 +68,7 @@ def frames_to_device(x: np.ndarray, layout: int, device, stream: int) -> tuple[t
     padded, 16-byte aligned device buffer (padding atoms zeroed).  Returns
     (buffer, n_padded).  With pageable host access a kernel reads the numpy
     memory directly; otherwise a strided cudaMemcpy2DAsync is used."""
+    src = x
     x = np.ascontiguousarray(x, dtype=np.float32)
     F = x.shape[0]
     A = x.shape[1] if layout == _lib.ATOM_MAJOR else x.shape[2]
@@ -78,6 +79,11 @@ def frames_to_device(x: np.ndarray, layout: int, device, stream: int) -> tuple[t
         rows, hrow, drow = _rows(layout, F, A)
         if pageable_access():
             check(lib.gbrmsd_copy_rows_kernel(buf.data_ptr(), drow, x.ctypes.data, hrow, hrow, drow, rows, stream))
+            if x is not src:
+                # the kernel reads the host array asynchronously: a converted
+                # copy made here must outlive it (the caller's own array is
+                # the caller's to keep alive until it synchronises)
+                torch.cuda.synchronize(device)
         else:
             copy_rows(buf.data_ptr(), drow * 4, x.ctypes.data, hrow * 4, hrow * 4, rows, 1, stream)
     return buf, Ap

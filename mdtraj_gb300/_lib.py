@@ -52,6 +52,13 @@ SIGNATURES: dict[str, tuple] = {
     "gbrmsd_allpairs_workspace_bytes": (_sz, [_i64, _i32]),
     "gbrmsd_allpairs": (C.c_int, [_vp, _i64, _i32, _i32, _i64, _i32, _i32, _i32, _vp, _vp, _sz, _vp]),
     "gbrmsd_allpairs_status": (C.c_int, [_vp, _vp, _vp]),
+    "gbrmsd_rotations_workspace_bytes": (_sz, [_i64, _i32]),
+    "gbrmsd_rotations": (C.c_int, [_vp, _i64, _i32, _i32, _i64, _i32, _i32, _vp, _vp, C.c_float, _vp, _vp, _vp, _vp,
+                                   _sz, _vp]),
+    "gbrmsd_apply_rotations": (C.c_int, [_vp, _i64, _i32, _i64, _vp, _vp, _vp, _vp, _vp]),
+    "gbrmsd_rmsf_workspace_bytes": (_sz, [_i64, _i32]),
+    "gbrmsd_rmsf": (C.c_int, [_vp, _i64, _i32, _i64, _vp, _vp, _vp, _sz, _vp]),
+    "gbrmsd_rotated_rmsd": (C.c_int, [_vp, _i64, _i32, _i64, _vp, _vp, _vp, _vp]),
     "gbrmsd_frameset_bytes": (_sz, [_i64, _i32]),
     "gbrmsd_frameset_prepare": (C.c_int, [_vp, _i64, _i32, _i32, _i64, _i32, _i32, _vp, _i64, _i64, _vp]),
     "gbrmsd_cross_workspace_bytes": (_sz, [_i64, _i64, _i32]),

@@ -256,3 +256,8 @@ def _center_inplace_atom_major(xyz):
     traces = D.center_inplace(x_dev, n_frames, n_atoms, n_padded, _lib.ATOM_MAJOR)
     D.frames_to_host(x_dev, xyz, _lib.ATOM_MAJOR, n_atoms, n_padded, stream)
     return D.to_host(traces, stream)
+
+
+# superposition entry points of the same module (_rmsd.pyx:246-759); imported
+# last because they use the argument coercions above
+from .superpose import getMultipleAlignDisplaceRMSDs_atom_major, rmsf, superpose_atom_major  # noqa: E402,F401

@@ -328,6 +328,8 @@ __global__ void __launch_bounds__(256) ragged_finish_kernel(const RaggedFinishAr
   c.out_idx = gf;
   c.refine_frame = gf;
   c.refine_seg = s;
+  c.out_rot = nullptr;
+  c.out_mu = nullptr;
   finish_frame(c, a.out, nullptr, nullptr, a.refine, a.refine_count, a.err);
 }
 

@@ -346,6 +346,8 @@ __global__ void __launch_bounds__(256) finish_kernel(const FinishArgs a) {
   c.out_idx = f;
   c.refine_frame = f;
   c.refine_seg = 0;
+  c.out_rot = a.out_rot;
+  c.out_mu = a.out_mu;
   finish_frame(c, a.out_rmsd, a.out_centroid, a.out_trace, a.refine, a.refine_count, a.err);
 }
 
@@ -735,6 +737,12 @@ int gbrmsd_reference_info(const void* ref_ws, float* host_trace, float* host_cen
   return GBRMSD_OK;
 }
 
+size_t gbrmsd_rotations_workspace_bytes(int64_t n_frames, int32_t n_atoms) {
+  if (n_frames < 0 || n_atoms < 0) return 0;
+  return align_up(ws_layout(n_frames, rmsd_splits_max(n_frames, n_atoms)).total, 256) +
+         align_up((size_t)n_frames * sizeof(float), 256);
+}
+
 size_t gbrmsd_rmsd_workspace_bytes(int64_t n_frames, int32_t n_atoms) {
   if (n_frames < 0 || n_atoms < 0) return 0;
   return ws_layout(n_frames, rmsd_splits_max(n_frames, n_atoms)).total;
@@ -805,6 +813,8 @@ int gbrmsd_rmsd_to_reference(const float* x, int64_t n_frames, int32_t n_atoms, 
   fa.refine_count = &hdr->refine_count;
   fa.err = &hdr->err;
   fa.mode = mode;
+  fa.out_rot = nullptr;
+  fa.out_mu = nullptr;
   const int fb = (int)((n_frames + 255) / 256);
   finish_kernel<<<fb, 256, 0, st>>>(fa);
   GB_CUDA_TRY(cudaGetLastError(), "launch finish_kernel");
@@ -825,6 +835,82 @@ int gbrmsd_rmsd_to_reference(const float* x, int64_t n_frames, int32_t n_atoms, 
     else
       refine_kernel<AXIS_MAJOR><<<rgrid, 256, 0, st>>>(ra);
     GB_CUDA_TRY(cudaGetLastError(), "launch refine_kernel");
+  }
+  return GBRMSD_OK;
+}
+
+int gbrmsd_rotations(const float* x, int64_t n_frames, int32_t n_atoms, int32_t n_padded, int64_t frame_stride,
+                     int32_t layout, int32_t mode, const void* ref_ws, const float* g_target, float g_ref,
+                     float* out_rot, double* out_centroid, float* out_rmsd, void* ws, size_t ws_bytes,
+                     void* stream) {
+  clear_error();
+  int rc = check_frames(x, n_frames, n_atoms, n_padded, frame_stride, layout);
+  if (rc) return rc;
+  if (mode != MODE_CENTER && mode != MODE_PRECENTERED)
+    return set_error(GBRMSD_E_INVALID, "rotations: mode must be CENTER or PRECENTERED");
+  if (n_frames == 0) return GBRMSD_OK;
+  if (!out_rot || !ref_ws) return set_error(GBRMSD_E_INVALID, "rotations: null out_rot or reference workspace");
+  if (mode == MODE_PRECENTERED && !g_target) return set_error(GBRMSD_E_INVALID, "precentered mode needs g_target");
+  if (n_atoms == 0) return set_error(GBRMSD_E_INVALID, "rotations: need at least one alignment atom");
+  const StreamCfg cfg = choose_cfg(n_padded, true);
+  const int32_t S = choose_splits(n_frames, (n_atoms + 3) / 4, grid_warps(cfg));
+  const WsLayout L = ws_layout(n_frames, S);
+  const size_t scratch_off = align_up(L.total, 256);
+  if (!ws || ws_bytes < scratch_off + align_up((size_t)n_frames * sizeof(float), 256) || !aligned16(ws))
+    return set_error(GBRMSD_E_WORKSPACE, "rotations: workspace needs %zu bytes (16-byte aligned)",
+                     scratch_off + align_up((size_t)n_frames * sizeof(float), 256));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const RefWsLayout RL = ref_ws_layout(n_atoms, n_padded);
+  const unsigned char* rw = static_cast<const unsigned char*>(ref_ws);
+  unsigned char* w = static_cast<unsigned char*>(ws);
+  WsHeader* hdr = reinterpret_cast<WsHeader*>(w);
+  GB_CUDA_TRY(cudaMemsetAsync(hdr, 0, sizeof(WsHeader), st), "memset workspace header");
+  StreamArgs sa;
+  sa.x = x;
+  sa.n_frames = n_frames;
+  sa.n_atoms = n_atoms;
+  sa.n_padded = n_padded;
+  sa.frame_stride = frame_stride;
+  sa.ref = reinterpret_cast<const float*>(rw + RL.coords_off);
+  sa.splits = S;
+  sa.sums = reinterpret_cast<double*>(w + L.sums_off);
+  sa.err = &hdr->err;
+  rc = launch_stream(layout, mode, sa, cfg, st);
+  if (rc) return rc;
+  FinishArgs fa{};
+  fa.n_frames = n_frames;
+  fa.n_atoms = n_atoms;
+  fa.splits = S;
+  fa.sums = sa.sums;
+  fa.ref_info = reinterpret_cast<const RefInfo*>(rw + RL.info_off);
+  fa.ref_prefix = reinterpret_cast<const double*>(rw + RL.prefix_off);
+  fa.g_target = g_target;
+  fa.g_ref_override = g_ref;
+  fa.self_index = -1;
+  fa.out_rmsd = out_rmsd ? out_rmsd : reinterpret_cast<float*>(w + scratch_off);
+  fa.refine = reinterpret_cast<RefineEntry*>(w + L.refine_off);
+  fa.refine_count = &hdr->refine_count;
+  fa.err = &hdr->err;
+  fa.mode = mode;
+  fa.out_rot = out_rot;
+  fa.out_mu = mode == MODE_CENTER ? out_centroid : nullptr;
+  finish_kernel<<<(int)((n_frames + 255) / 256), 256, 0, st>>>(fa);
+  GB_CUDA_TRY(cudaGetLastError(), "launch finish_kernel (rotations)");
+  if (out_rmsd) {  // exact rmsd for near-identical frames, as gbrmsd_rmsd_to_reference
+    RefineArgs ra;
+    ra.x = x;
+    ra.n_atoms = n_atoms;
+    ra.n_padded = n_padded;
+    ra.frame_stride = frame_stride;
+    ra.ref = sa.ref;
+    ra.list = fa.refine;
+    ra.count = fa.refine_count;
+    ra.out_rmsd = out_rmsd;
+    if (layout == ATOM_MAJOR)
+      refine_kernel<ATOM_MAJOR><<<sm_count() * 4, 256, 0, st>>>(ra);
+    else
+      refine_kernel<AXIS_MAJOR><<<sm_count() * 4, 256, 0, st>>>(ra);
+    GB_CUDA_TRY(cudaGetLastError(), "launch refine_kernel (rotations)");
   }
   return GBRMSD_OK;
 }

@@ -68,6 +68,8 @@ struct FinishArgs {
   int* refine_count;
   int* err;
   int32_t mode;
+  float* out_rot;             // optional, n_frames x 9 (superposition)
+  double* out_mu;             // optional with out_rot, n_frames x 3
 };
 
 }  // namespace gb

@@ -239,6 +239,8 @@ struct FrameCtx {
   int64_t out_idx;         // index into the outputs
   int64_t refine_frame;    // frame id recorded for refinement
   int32_t refine_seg;      // segment id recorded for refinement (ragged)
+  float* out_rot;          // optional: rotation R (row-major, R (a - mu) ~ b) per frame, 9 floats
+  double* out_mu;          // optional with out_rot: FP64 centroid per frame, 3 doubles
 };
 
 __device__ __forceinline__ void finish_frame(const FrameCtx& c, float* out_rmsd, float* out_centroid,
@@ -305,7 +307,7 @@ __device__ __forceinline__ void finish_frame(const FrameCtx& c, float* out_rmsd,
 
   bool self = c.self;
   if (self && c.mode == MODE_PRECENTERED) self = (c.g_target == c.g_ref);
-  if (self) {
+  if (self && !c.out_rot) {  // a rotation is still computed for superposition
     out_rmsd[f] = 0.f;
     return;
   }
@@ -314,13 +316,23 @@ __device__ __forceinline__ void finish_frame(const FrameCtx& c, float* out_rmsd,
   if (!finite) {
     atomicOr(err, DEV_ERR_NONFINITE);
     out_rmsd[f] = nanf("");
+    if (c.out_rot)
+      for (int i = 0; i < 9; ++i) c.out_rot[9 * f + i] = nanf("");
     return;
   }
   int iters = 0;
   const double lam = qcp_lambda_max_mixed(m, ga, gb, &iters);
   double msd = (ga + gb - 2.0 * lam) / dA;
-  if (!(msd > 0.0)) msd = 0.0;
+  if (!(msd > 0.0) || self) msd = 0.0;
   out_rmsd[f] = sqrtf((float)msd);
+  if (c.out_rot) {
+    double rot[9];
+    qcp_rotation(m, lam, rot);
+    for (int i = 0; i < 9; ++i) c.out_rot[9 * f + i] = (float)rot[i];
+    if (c.out_mu)
+      for (int k = 0; k < 3; ++k) c.out_mu[3 * f + k] = mu[k];
+  }
+  if (self) return;
 
   // One-pass sums resolve msd to about 1e-7 * scale / sqrt(A); below
   // (0.1 * scale / sqrt(A))^2 the direct residual is recomputed by the

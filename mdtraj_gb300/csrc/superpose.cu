@@ -1,0 +1,289 @@
+// Superposition on GB300: applying per-frame rotations, RMSF, and the
+// rotated (align-on-one-set, measure-on-another) MSD.
+//
+//   apply_rotations_kernel  x <- R_f (x - mu_f) + offset for every atom of every
+//                           frame, in place (Trajectory.superpose,
+//                           mdtraj/core/trajectory.py:1127-1165, with
+//                           rot_atom_major, src/rotation_generic.h:29-44)
+//   rmsf_partial_kernel     per (frame chunk, atom): compensated sums of the
+//   rmsf_final_kernel       rotated positions about a per-atom shift, then the
+//                           mean and mean squared deviation per atom (rmsf,
+//                           mdtraj/rmsd/_rmsd.pyx:419-451)
+//   rotated_msd_kernel      warp per frame: sum |R_f a_k - b_k|^2 / n
+//                           (rot_msd_atom_major, src/rotation_generic.h:47-103,
+//                           as used by getMultipleAlignDisplaceRMSDs_atom_major,
+//                           _rmsd.pyx:677-759)
+//
+// Rotations come from gbrmsd_rotations (row-major R, aligned = R x).  All
+// three kernels are HBM-bound streaming passes over float32 coordinates.
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+
+#include "capi_internal.h"
+#include "common.cuh"
+
+namespace gb {
+namespace {
+
+// float(double(x) + d) computed in FP32 from the split d = hi + lo (hi =
+// float(d), lo = float(d - hi)): within one float ulp of the FP64 form and free
+// of GB300's slow FP64 pipe.
+__device__ __forceinline__ float add_split(float x, float hi, float lo) { return (x + hi) + lo; }
+
+constexpr int APPLY_THREADS = 256;
+
+__global__ void __launch_bounds__(APPLY_THREADS) apply_rotations_kernel(float* __restrict__ x, int64_t F, int32_t A,
+                                                                       int64_t fs, const float* __restrict__ rot,
+                                                                       const double* __restrict__ mu, double o0,
+                                                                       double o1, double o2, int32_t* nonzero0) {
+  const int32_t nab = (A + APPLY_THREADS - 1) / APPLY_THREADS;
+  const int64_t f = blockIdx.x / nab;
+  const int32_t k = (int32_t)(blockIdx.x - f * nab) * APPLY_THREADS + threadIdx.x;
+  if (f >= F) return;
+  float r[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) r[i] = rot[9 * f + i];
+  float mh[3] = {0.f, 0.f, 0.f}, ml[3] = {0.f, 0.f, 0.f};
+  if (mu) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const double m = mu[3 * f + c];
+      mh[c] = -(float)m;
+      ml[c] = -(float)(m + (double)mh[c]);
+    }
+  }
+  const float oh[3] = {(float)o0, (float)o1, (float)o2};
+  const float ol[3] = {(float)(o0 - (double)oh[0]), (float)(o1 - (double)oh[1]), (float)(o2 - (double)oh[2])};
+  bool nz = false;
+  if (k < A) {
+    float* p = x + f * fs + 3 * (int64_t)k;
+    const float dx = add_split(p[0], mh[0], ml[0]);
+    const float dy = add_split(p[1], mh[1], ml[1]);
+    const float dz = add_split(p[2], mh[2], ml[2]);
+    const float rx = fmaf(r[0], dx, fmaf(r[1], dy, r[2] * dz));
+    const float ry = fmaf(r[3], dx, fmaf(r[4], dy, r[5] * dz));
+    const float rz = fmaf(r[6], dx, fmaf(r[7], dy, r[8] * dz));
+    nz = (rx != 0.f) || (ry != 0.f) || (rz != 0.f);
+    p[0] = add_split(rx, oh[0], ol[0]);
+    p[1] = add_split(ry, oh[1], ol[1]);
+    p[2] = add_split(rz, oh[2], ol[2]);
+  }
+  if (nonzero0 && f == 0 && __any_sync(FULL_MASK, nz) && (threadIdx.x & 31) == 0) atomicOr(nonzero0, 1);
+}
+
+// ---- RMSF ---------------------------------------------------------------
+
+constexpr int RMSF_THREADS = 128;
+constexpr int RMSF_FOLD = 16;  // frames per FP32 partial before it is folded into a TwoSum pair
+
+__device__ __forceinline__ void rotate(const float* r, float ax, float ay, float az, float& bx, float& by, float& bz) {
+  bx = fmaf(r[0], ax, fmaf(r[1], ay, r[2] * az));
+  by = fmaf(r[3], ax, fmaf(r[4], ay, r[5] * az));
+  bz = fmaf(r[6], ax, fmaf(r[7], ay, r[8] * az));
+}
+
+// part[(chunk * A + k) * 4 + {0,1,2,3}] = sums over the chunk's frames of
+// d = R_f x_fk - s_k (3 components) and |d|^2, s_k = R_0 x_0k.
+__global__ void __launch_bounds__(RMSF_THREADS) rmsf_partial_kernel(const float* __restrict__ x, int64_t F, int32_t A,
+                                                                   int64_t fs, const float* __restrict__ rot,
+                                                                   int64_t fch, double* __restrict__ part) {
+  __shared__ float sr[RMSF_FOLD * 9];
+  const int32_t k = blockIdx.x * RMSF_THREADS + threadIdx.x;
+  const int64_t f0 = (int64_t)blockIdx.y * fch;
+  const int64_t f1 = min(F, f0 + fch);
+  float s[3] = {0.f, 0.f, 0.f};
+  if (k < A) {
+    const float* p = x + 3 * (int64_t)k;
+    if (rot) rotate(rot, p[0], p[1], p[2], s[0], s[1], s[2]);
+    else { s[0] = p[0]; s[1] = p[1]; s[2] = p[2]; }
+  }
+  CF acc[4] = {cf_zero(), cf_zero(), cf_zero(), cf_zero()};
+  for (int64_t fb = f0; fb < f1; fb += RMSF_FOLD) {
+    const int nf = (int)(f1 - fb < RMSF_FOLD ? f1 - fb : RMSF_FOLD);
+    __syncthreads();
+    if (rot)
+      for (int t = threadIdx.x; t < nf * 9; t += RMSF_THREADS) sr[t] = rot[9 * fb + t];
+    __syncthreads();
+    float a[4] = {0.f, 0.f, 0.f, 0.f};
+    if (k < A) {
+      for (int i = 0; i < nf; ++i) {
+        const float* p = x + (fb + i) * fs + 3 * (int64_t)k;
+        float bx = p[0], by = p[1], bz = p[2];
+        if (rot) rotate(sr + 9 * i, p[0], p[1], p[2], bx, by, bz);
+        const float dx = bx - s[0], dy = by - s[1], dz = bz - s[2];
+        a[0] += dx;
+        a[1] += dy;
+        a[2] += dz;
+        a[3] = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, a[3])));
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) cf_add(acc[j], a[j]);
+  }
+  if (k < A) {
+    double* o = part + ((int64_t)blockIdx.y * A + k) * 4;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) o[j] = cf_to_double(acc[j]);
+  }
+}
+
+__global__ void __launch_bounds__(256) rmsf_final_kernel(const double* __restrict__ part, int32_t n_chunks, int32_t A,
+                                                        int64_t F, float* __restrict__ out) {
+  const int32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= A) return;
+  double t[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int32_t c = 0; c < n_chunks; ++c)
+    for (int j = 0; j < 4; ++j) t[j] += part[((int64_t)c * A + k) * 4 + j];
+  const double inv = 1.0 / (double)F;
+  const double mx = t[0] * inv, my = t[1] * inv, mz = t[2] * inv;
+  double var = t[3] * inv - (mx * mx + my * my + mz * mz);
+  if (!(var > 0.0)) var = 0.0;
+  out[k] = (float)sqrt(var);
+}
+
+struct RmsfPlan {
+  int64_t fch;
+  int32_t n_chunks;
+  size_t bytes;
+};
+
+RmsfPlan rmsf_plan(int64_t F, int32_t A) {
+  RmsfPlan p;
+  // enough frame chunks to fill the GPU when there are few atoms, at most 65,535
+  const int64_t atom_blocks = ((int64_t)A + RMSF_THREADS - 1) / RMSF_THREADS;
+  int64_t want = (8LL * 152 + atom_blocks - 1) / (atom_blocks > 0 ? atom_blocks : 1);
+  if (want < 1) want = 1;
+  int64_t fch = (F + want - 1) / want;
+  if (fch < 64) fch = 64;
+  if ((F + fch - 1) / fch > 65535) fch = (F + 65534) / 65535;
+  p.fch = fch;
+  p.n_chunks = (int32_t)((F + fch - 1) / fch);
+  if (p.n_chunks < 1) p.n_chunks = 1;
+  p.bytes = align_up((size_t)p.n_chunks * (size_t)A * 4 * sizeof(double), 256);
+  return p;
+}
+
+// ---- rotated MSD (align-displace) -----------------------------------------
+
+__global__ void __launch_bounds__(256) rotated_msd_kernel(const float* __restrict__ x, int64_t F, int32_t A,
+                                                         int64_t fs, const float* __restrict__ rot,
+                                                         const float* __restrict__ ref, float* __restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const int64_t W = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t f = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); f < F; f += W) {
+    float r[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) r[i] = rot[9 * f + i];
+    const float* p = x + f * fs;
+    CF acc = cf_zero();
+    for (int32_t k0 = 0; k0 < A; k0 += 32 * 8) {
+      float part = 0.f;
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int32_t k = k0 + lane + 32 * u;
+        if (k < A) {
+          float bx, by, bz;
+          rotate(r, p[3 * k], p[3 * k + 1], p[3 * k + 2], bx, by, bz);
+          const float dx = bx - ref[3 * k], dy = by - ref[3 * k + 1], dz = bz - ref[3 * k + 2];
+          part = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, part)));
+        }
+      }
+      cf_add(acc, part);
+    }
+#pragma unroll
+    for (int m = 16; m >= 1; m >>= 1) {
+      CF o;
+      o.hi = __shfl_xor_sync(FULL_MASK, acc.hi, m);
+      o.lo = __shfl_xor_sync(FULL_MASK, acc.lo, m);
+      acc = cf_add2(acc, o);
+    }
+    if (lane == 0) {
+      double msd = A > 0 ? cf_to_double(acc) / (double)A : 0.0;
+      if (!(msd > 0.0)) msd = (msd == msd) ? 0.0 : msd;
+      out[f] = sqrtf((float)msd);
+    }
+  }
+}
+
+int check_rows(const void* x, int64_t F, int32_t A, int64_t fs, const char* who) {
+  if (F < 0 || A < 0) return set_error(GBRMSD_E_INVALID, "%s: negative sizes", who);
+  if (fs < 3LL * A) return set_error(GBRMSD_E_INVALID, "%s: frame_stride must be >= 3 * n_atoms", who);
+  if (F > 0 && A > 0 && !x) return set_error(GBRMSD_E_INVALID, "%s: null coordinates", who);
+  return GBRMSD_OK;
+}
+
+}  // namespace
+}  // namespace gb
+
+using namespace gb;
+
+extern "C" {
+
+int gbrmsd_apply_rotations(float* x, int64_t n_frames, int32_t n_atoms, int64_t frame_stride, const float* rot,
+                           const double* centroids, const double* offset3, int32_t* nonzero0, void* stream) {
+  clear_error();
+  int rc = check_rows(x, n_frames, n_atoms, frame_stride, "apply_rotations");
+  if (rc) return rc;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (nonzero0) GB_CUDA_TRY(cudaMemsetAsync(nonzero0, 0, sizeof(int32_t), st), "memset nonzero flag");
+  if (n_frames == 0 || n_atoms == 0) return GBRMSD_OK;
+  if (!rot) return set_error(GBRMSD_E_INVALID, "apply_rotations: null rotations");
+  const int64_t nab = (n_atoms + APPLY_THREADS - 1) / APPLY_THREADS;
+  if (n_frames * nab > 0x7fffffffLL) return set_error(GBRMSD_E_INVALID, "apply_rotations: too many frames");
+  const double o0 = offset3 ? offset3[0] : 0.0, o1 = offset3 ? offset3[1] : 0.0, o2 = offset3 ? offset3[2] : 0.0;
+  apply_rotations_kernel<<<(unsigned)(n_frames * nab), APPLY_THREADS, 0, st>>>(x, n_frames, n_atoms, frame_stride, rot,
+                                                                               centroids, o0, o1, o2, nonzero0);
+  GB_CUDA_TRY(cudaGetLastError(), "launch apply_rotations_kernel");
+  return GBRMSD_OK;
+}
+
+size_t gbrmsd_rmsf_workspace_bytes(int64_t n_frames, int32_t n_atoms) {
+  if (n_frames < 0 || n_atoms < 0) return 0;
+  return rmsf_plan(n_frames, n_atoms).bytes;
+}
+
+int gbrmsd_rmsf(const float* x, int64_t n_frames, int32_t n_atoms, int64_t frame_stride, const float* rot,
+                float* out_rmsf, void* ws, size_t ws_bytes, void* stream) {
+  clear_error();
+  int rc = check_rows(x, n_frames, n_atoms, frame_stride, "rmsf");
+  if (rc) return rc;
+  if (n_atoms == 0) return GBRMSD_OK;
+  if (!out_rmsf) return set_error(GBRMSD_E_INVALID, "rmsf: null output");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (n_frames == 0) {
+    // the reference divides the zero sums by n_frames: 0/0 -> NaN
+    return set_error(GBRMSD_E_INVALID, "rmsf: need at least one frame");
+  }
+  const RmsfPlan P = rmsf_plan(n_frames, n_atoms);
+  if (!ws || ws_bytes < P.bytes) return set_error(GBRMSD_E_WORKSPACE, "rmsf: workspace needs %zu bytes", P.bytes);
+  double* part = static_cast<double*>(ws);
+  dim3 grid((unsigned)((n_atoms + RMSF_THREADS - 1) / RMSF_THREADS), (unsigned)P.n_chunks);
+  prof_begin(st);
+  rmsf_partial_kernel<<<grid, RMSF_THREADS, 0, st>>>(x, n_frames, n_atoms, frame_stride, rot, P.fch, part);
+  GB_CUDA_TRY(cudaGetLastError(), "launch rmsf_partial_kernel");
+  prof_end(st);
+  rmsf_final_kernel<<<(n_atoms + 255) / 256, 256, 0, st>>>(part, P.n_chunks, n_atoms, n_frames, out_rmsf);
+  GB_CUDA_TRY(cudaGetLastError(), "launch rmsf_final_kernel");
+  return GBRMSD_OK;
+}
+
+int gbrmsd_rotated_rmsd(const float* x, int64_t n_frames, int32_t n_atoms, int64_t frame_stride, const float* rot,
+                        const float* ref_frame, float* out_rmsd, void* stream) {
+  clear_error();
+  int rc = check_rows(x, n_frames, n_atoms, frame_stride, "rotated_rmsd");
+  if (rc) return rc;
+  if (n_frames == 0) return GBRMSD_OK;
+  if (!rot || !out_rmsd || (n_atoms > 0 && !ref_frame))
+    return set_error(GBRMSD_E_INVALID, "rotated_rmsd: null rotations, reference or output");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int64_t warps = (int64_t)sm_count() * 32;
+  const int64_t blocks = std::min<int64_t>((n_frames + 7) / 8, warps / 8);
+  rotated_msd_kernel<<<(unsigned)(blocks > 0 ? blocks : 1), 256, 0, st>>>(x, n_frames, n_atoms, frame_stride, rot,
+                                                                          ref_frame, out_rmsd);
+  GB_CUDA_TRY(cudaGetLastError(), "launch rotated_msd_kernel");
+  return GBRMSD_OK;
+}
+
+}  // extern "C"

@@ -71,3 +71,10 @@ class Trajectory:
             raise NotImplementedError("mass-weighted centring needs atom masses from a topology")
         self._rmsd_traces = _center_inplace_atom_major(self._xyz)
         return self
+
+    def superpose(self, reference, frame=0, atom_indices=None, ref_atom_indices=None, parallel=True):
+        """Superposes each conformation upon frame ``frame`` of ``reference``
+        in place (core/trajectory.py:1083-1170); returns self."""
+        from .superpose import superpose
+
+        return superpose(self, reference, frame, atom_indices, ref_atom_indices, parallel)

@@ -61,3 +61,69 @@ def msd_nosuperpose(frames: np.ndarray, ref: np.ndarray) -> np.ndarray:
     (mdtraj/rmsd/_rmsd.pyx:762-793)."""
     d = np.asarray(frames, dtype=np.float64) - np.asarray(ref, dtype=np.float64)[None]
     return np.sqrt((d * d).sum(axis=(1, 2)) / max(frames.shape[1], 1))
+
+
+def kabsch_rotations(frames: np.ndarray, ref: np.ndarray, centre: bool = True) -> np.ndarray:
+    """Optimal rotations R (F, 3, 3), float64, with R (a - mean a) the frame
+    aligned onto (ref - mean ref) (alignment.py:117-181 with the reflection
+    fix).  centre=False uses the coordinates as given."""
+    a = np.asarray(frames, dtype=np.float64)
+    b = np.asarray(ref, dtype=np.float64)
+    if centre:
+        a = a - a.mean(1, keepdims=True)
+        b = b - b.mean(0)
+    corr = np.einsum("fki,kj->fij", a, b)                  # sum a b^T
+    V, S, Wt = np.linalg.svd(corr)
+    d = np.sign(np.linalg.det(V) * np.linalg.det(Wt))
+    D = np.repeat(np.eye(3)[None], a.shape[0], 0)
+    D[:, 2, 2] = d
+    # maximise tr(R corr): R = W D V^T
+    return np.einsum("fji,fjk,flk->fil", Wt, D, V)
+
+
+def superpose(frames: np.ndarray, ref_frame: np.ndarray, align=None, ref_align=None) -> np.ndarray:
+    """FP64 Trajectory.superpose (core/trajectory.py:1083-1170): every frame
+    centred on the centroid of its alignment atoms, rotated onto the centred
+    reference alignment atoms, translated onto the reference centroid."""
+    x = np.asarray(frames, dtype=np.float64)
+    ai = slice(None) if align is None else align
+    ri = ai if ref_align is None else ref_align
+    xa = x[:, ai]
+    r = np.asarray(ref_frame, dtype=np.float64)[ri]
+    mu = xa.mean(1, keepdims=True)
+    rmu = r.mean(0)
+    R = kabsch_rotations(xa - mu, r - rmu, centre=False)
+    return np.einsum("fij,fkj->fki", R, x - mu) + rmu
+
+
+def rmsf(target: np.ndarray, ref_frame: np.ndarray | None, atom_indices=None, ref_atom_indices=None) -> np.ndarray:
+    """FP64 rmsf following the reference's data flow (_rmsd.pyx:246-484):
+    rotations from the centred selection onto the centred reference frame; they
+    are applied about the origin to the centred selection when atom_indices is
+    None, to the original (uncentred) selection otherwise; ref_frame None
+    means no rotation; the reference frame is restricted to ref_atom_indices
+    (default atom_indices).  Then the per-atom RMS deviation from the mean."""
+    x = np.asarray(target, dtype=np.float64)
+    sel = x if atom_indices is None else x[:, atom_indices]
+    c = sel - sel.mean(1, keepdims=True)
+    disp = c if atom_indices is None else sel
+    if ref_frame is not None:
+        r = np.asarray(ref_frame, dtype=np.float64)
+        ri = atom_indices if ref_atom_indices is None else ref_atom_indices
+        if ri is not None:
+            r = r[ri]
+        R = kabsch_rotations(c, r - r.mean(0), centre=False)
+        disp = np.einsum("fij,fkj->fki", R, disp)
+    mean = disp.mean(0)
+    return np.sqrt(((disp - mean) ** 2).sum(2).mean(0))
+
+
+def align_displace(align_ref: np.ndarray, align: np.ndarray, displ_ref: np.ndarray, displ: np.ndarray):
+    """FP64 getMultipleAlignDisplaceRMSDs_atom_major (_rmsd.pyx:677-759) on the
+    real atoms: R aligns each frame's (pre-centred) alignment atoms onto the
+    reference frame's, rmsd = sqrt(mean |R displ_k - displ_ref_k|^2).  Returns
+    (rmsd (F,), R (F, 3, 3))."""
+    R = kabsch_rotations(align, align_ref, centre=False)
+    d = np.einsum("fij,fkj->fki", R, np.asarray(displ, dtype=np.float64)) - np.asarray(displ_ref, dtype=np.float64)
+    n = max(displ.shape[1], 1)
+    return np.sqrt((d * d).sum((1, 2)) / n), R

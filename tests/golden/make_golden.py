@@ -18,6 +18,12 @@ through a stub ``mdtraj`` package, and records:
 * synthetic.npz   — small seeded cases (odd atom counts, exact copies,
                     degenerate 1-3 atom frames, atom_indices subsets,
                     superpose=False) with the reference's outputs.
+* superpose_rmsf.npz — Trajectory.superpose (all atoms, a subset, another
+                    reference object with shifted indices), rmsf (against
+                    the trajectory itself, None, a subset, another reference,
+                    with the in-place centring side effects) and
+                    getMultipleAlignDisplaceRMSDs_atom_major (distances and
+                    rotation matrices), all from the reference.
 
 Usage:  python tests/golden/make_golden.py
 """
@@ -201,12 +207,100 @@ def synthetic_fixture(_rmsd) -> None:
     np.savez_compressed(OUT / "synthetic.npz", **arrays)
 
 
+def ref_superpose(_rmsd, xyz, ref_xyz, frame, ai=None, rai=None):
+    """Trajectory.superpose (core/trajectory.py:1113-1165 is plain numpy around
+    the compiled superpose_atom_major, and core/ is not importable here):
+    centre on the alignment atoms' float64 mean, centre the reference frame,
+    float32 traces, the compiled rotation, then add the reference offset."""
+    ai = slice(None) if ai is None else ai
+    rai = ai if rai is None else rai
+    x = np.array(xyz, dtype=np.float32, copy=True, order="C")
+    align = np.asarray(x[:, ai, :], order="c")
+    ref_align = np.array(ref_xyz[frame, rai, :], dtype=np.float32, copy=True, order="c").reshape(1, -1, 3)
+    offset = np.mean(align, axis=1, dtype=np.float64).reshape(len(x), 1, 3)
+    align -= offset
+    if align.ctypes.data != x.ctypes.data:
+        x -= offset
+    ref_offset = ref_align[0].astype("float64").mean(0)
+    ref_align[0] -= ref_offset
+    g = np.einsum("ijk,ijk->i", align, align)
+    ref_g = np.einsum("ijk,ijk->i", ref_align, ref_align)
+    _rmsd.superpose_atom_major(ref_align, align, ref_g, g, x, 0)
+    x += ref_offset
+    return x
+
+
+def superpose_fixture(_rmsd) -> None:
+    """superpose_rmsf.npz: Trajectory.superpose, rmsf and
+    getMultipleAlignDisplaceRMSDs_atom_major from the reference."""
+    from mdtraj_gb300 import synth
+
+    ref, x = synth.single_reference_frames(30, 45, seed=31, sigma=0.2)
+    # another reference object: noisy, rotated, translated copies of frames
+    # 0-5 (atom k corresponds to atom k), and the same rolled by one atom
+    # (atom k + 1 corresponds to atom k, for shifted reference indices)
+    rng = np.random.default_rng(32)
+    rot = synth.haar_rotations(6, rng)
+    other = (np.einsum("fkj,fij->fki", x[:6].astype(np.float64) + rng.normal(size=(6, 45, 3)) * 0.05, rot)
+             + rng.uniform(-2, 2, size=(6, 1, 3))).astype(np.float32)
+    rolled = np.ascontiguousarray(np.roll(other, 1, axis=1))
+    # selections of 16 atoms: the reference's vectorised msd_atom_major reads
+    # whole 4-atom groups, so with a selection whose size is not a multiple of
+    # 4 it reads past the end of the selected reference frame (rmsf and
+    # superpose_atom_major pass the selection size as the padded size) and its
+    # results change from call to call
+    sub = np.arange(0, 32, 2)
+    shifted = sub + 1
+    arrays = {"xyz": x, "other": other, "rolled": rolled, "sub": sub, "shifted": shifted}
+    arrays["sup_all_f3"] = ref_superpose(_rmsd, x, x, 3)
+    arrays["sup_sub_f0"] = ref_superpose(_rmsd, x, x, 0, sub)
+    arrays["sup_other_f2"] = ref_superpose(_rmsd, x, rolled, 2, sub, shifted)
+    # rmsf: each call centres its target (and the reference frame) in place
+    t = Traj(x.copy())
+    arrays["rmsf_self_f0"] = np.asarray(_rmsd.rmsf(t, t, 0), dtype=np.float32)
+    arrays["rmsf_self_f0_centred"] = t.xyz.copy()
+    t = Traj(x.copy())
+    arrays["rmsf_none"] = np.asarray(_rmsd.rmsf(t, None), dtype=np.float32)
+    # with an explicit atom_indices the reference's rmsf() returns values that
+    # change from call to call under OpenMP (measured here: the first atoms of
+    # the selection differ between runs and from the serial result); the pin
+    # for that case is the reference's own kernels composed along rmsf's data
+    # flow (_rmsd.pyx:389-418): centre a copy of the selection and the selected
+    # reference frame, rotate the uncentred selection about the origin
+    t = Traj(x.copy())
+    _rmsd.rmsf(t, Traj(x.copy()), 5, atom_indices=sub)
+    arrays["rmsf_sub_f5_xyz_after"] = t.xyz.copy()
+    sel = np.ascontiguousarray(x[:, sub])
+    g_sel = np.asarray(_rmsd._center_inplace_atom_major(sel), dtype=np.float32)
+    ref_sel = np.ascontiguousarray(x[5, sub])[None].copy()
+    g_ref = np.asarray(_rmsd._center_inplace_atom_major(ref_sel), dtype=np.float32)
+    disp = np.ascontiguousarray(x[:, sub]).copy()
+    _rmsd.superpose_atom_major(ref_sel, sel, g_ref, g_sel, disp, 0, parallel=False)
+    d = disp.astype(np.float64)
+    arrays["rmsf_sub_f5"] = np.sqrt(((d - d.mean(0)) ** 2).sum(2).mean(0)).astype(np.float32)
+    t = Traj(x.copy())
+    r = Traj(other.copy())
+    arrays["rmsf_other_f1"] = np.asarray(_rmsd.rmsf(t, r, 1), dtype=np.float32)
+    arrays["rmsf_other_f1_ref_after"] = r.xyz.copy()
+    # align-displace on padded, pre-centred alignment atoms
+    n_al, n_di = 21, 30
+    al = np.zeros((30, 24, 3), np.float32)
+    al[:, :n_al] = x[:, :n_al] - x[:, :n_al].astype(np.float64).mean(1, keepdims=True)
+    di = np.zeros((30, 32, 3), np.float32)
+    di[:, :n_di] = x[:, 15:45]
+    g = np.einsum("ijk,ijk->i", al, al).astype(np.float32)
+    d, rot = _rmsd.getMultipleAlignDisplaceRMSDs_atom_major(al, al, g, g, di, di, n_al, n_di, 4)
+    arrays.update(ad_align=al, ad_displ=di, ad_g=g, ad_rmsd=np.asarray(d, np.float32), ad_rot=np.asarray(rot, np.float32))
+    np.savez_compressed(OUT / "superpose_rmsf.npz", **arrays)
+
+
 def main() -> None:
     build_reference_python()
     _rmsd, xtc = import_reference()
     frame0_fixture(_rmsd, xtc)
     alignment_fixture()
     synthetic_fixture(_rmsd)
+    superpose_fixture(_rmsd)
     for p in sorted(OUT.glob("*.npz")):
         print(p.name, p.stat().st_size, "bytes")
 

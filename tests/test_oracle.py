@@ -68,3 +68,27 @@ def test_fp64_oracle_self_consistency():
     b = fp64.kabsch_rmsd_pairs(x, pairs)
     np.testing.assert_allclose(a, b, atol=1e-12)
     assert a[0] < 1e-12
+
+
+def test_fp64_superpose_rmsf_align_displace_match_reference(golden):
+    """The FP64 restatements of Trajectory.superpose, rmsf and
+    getMultipleAlignDisplaceRMSDs_atom_major against the reference's own
+    outputs (tests/golden/superpose_rmsf.npz)."""
+    g = golden("superpose_rmsf.npz")
+    x, other, rolled, sub, shifted = g["xyz"], g["other"], g["rolled"], g["sub"], g["shifted"]
+    assert np.abs(fp64.superpose(x, x[3]) - g["sup_all_f3"]).max() < 2e-5
+    assert np.abs(fp64.superpose(x, x[0], sub) - g["sup_sub_f0"]).max() < 2e-5
+    assert np.abs(fp64.superpose(x, rolled[2], sub, shifted) - g["sup_other_f2"]).max() < 2e-5
+    assert np.abs(fp64.rmsf(x, x[0]) - g["rmsf_self_f0"]).max() < 2e-5
+    assert np.abs(fp64.rmsf(x, None) - g["rmsf_none"]).max() < 2e-5
+    assert np.abs(fp64.rmsf(x, x[5], atom_indices=sub) - g["rmsf_sub_f5"]).max() < 2e-5
+    assert np.abs(fp64.rmsf(x, other[1]) - g["rmsf_other_f1"]).max() < 2e-5
+    # side effects recorded from the reference: centred target / reference frame
+    np.testing.assert_allclose(g["rmsf_self_f0_centred"].astype(np.float64).mean(1), 0.0, atol=1e-5)
+    np.testing.assert_array_equal(g["rmsf_sub_f5_xyz_after"], x)  # a subset is centred in a copy only
+    np.testing.assert_allclose(g["rmsf_other_f1_ref_after"][1].astype(np.float64).mean(0), 0.0, atol=1e-5)
+    al, di = g["ad_align"], g["ad_displ"]
+    d, R = fp64.align_displace(al[4, :21], al[:, :21], di[4, :30], di[:, :30])
+    assert np.abs(d - g["ad_rmsd"]).max() < 2e-5
+    # the reference's rotation array equals R (frame aligned onto the reference frame)
+    assert np.abs(R - g["ad_rot"]).max() < 2e-5
