@@ -48,6 +48,8 @@ WORKLOADS = {
     "allpairs_20000x2000": (20_000, 2_000, 50, 0.1, 5.0, 0.99),
     # ragged batch: (segments, atoms lo, atoms hi, frames lo, frames hi, sigma)
     "ragged_512": (512, 50, 20_000, 100, 5_000, 0.05),
+    # superposition / rmsf: (n_frames, n_atoms, sigma)
+    "superpose_100000x1000": (100_000, 1_000, 0.05),
     # serving: (database frames, atoms, offered rates (requests/s), max query frames, slice lengths)
     "serving_500000x300": (500_000, 300, (100, 300, 1000, 3000, 10000), 256, (10_000, 500_000)),
 }
@@ -952,6 +954,164 @@ def serving_cpu(dbs, F, A, q, budget_s, top) -> dict:
                       "pairs per request" % (reps, n, dt)}
 
 
+# ---------------------------------------------------------------------------
+# Superposition / RMSF workload
+# ---------------------------------------------------------------------------
+
+
+def run_superpose(args) -> dict:
+    """Trajectory.superpose(t, t, 0) and md.rmsf(t, t, 0) on 100,000 frames x
+    1,000 atoms generated as the single-reference workload (sigma 0.05 nm,
+    random rotations and translations).  One step = superposing the
+    device-resident frames onto frame 0: the rotation pass (streaming M + QCP
+    rotations) and the fused centre/rotate/translate pass, in place."""
+    import ctypes as C
+
+    import torch
+
+    import mdtraj_gb300 as md
+    from mdtraj_gb300 import _device as D
+    from mdtraj_gb300 import _lib, synth
+    from mdtraj_gb300.superpose import _rotations
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    F, A, sig = WORKLOADS[args.workload]
+    if args.frames:
+        F = args.frames
+    Ap = D.padded(A)
+    ref, x, _ = synth.device_single_reference(F, A, Ap, 0, seed=7 + rank, device=dev, sigma_lo=sig, sigma_hi=sig)
+    lib = _lib.lib
+    stream = D.stream_handle()
+    rng = np.random.default_rng(3)
+    sample = np.sort(rng.choice(F, size=min(F, 2000), replace=False))
+    before = x.view(F, Ap, 3)[torch.from_numpy(sample).to(dev), :A].cpu().numpy()
+    frame0 = x.view(F, Ap, 3)[0, :A].cpu().numpy()
+    ref_align = frame0.copy()
+    ref_offset = ref_align.astype(np.float64).mean(0)
+    ref_align -= ref_offset
+    dref = D.DeviceReference(ref_align, _lib.ATOM_MAJOR, centre=False, device=dev)
+    off = (C.c_double * 3)(*[float(v) for v in ref_offset])
+
+    def step():
+        rot, mu = _rotations(x, F, A, Ap, dref, _lib.MODE_CENTER, want_mu=True)
+        _lib.check(lib.gbrmsd_apply_rotations(x.data_ptr(), F, A, 3 * Ap, rot.data_ptr(), mu.data_ptr(), off, None,
+                                              stream))
+
+    step()
+    torch.cuda.synchronize()
+    after = x.view(F, Ap, 3)[torch.from_numpy(sample).to(dev), :A].cpu().numpy()
+    from oracle import fp64
+
+    want = fp64.superpose(before, frame0)
+    err = np.abs(after.astype(np.float64) - want)
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    with ClockSampler(local) as clk:
+        e[0].record()
+        for _ in range(args.steps):
+            step()
+        e[1].record()
+        torch.cuda.synchronize()
+    ms_step = e[0].elapsed_time(e[1]) / args.steps
+    # the two passes timed separately (same stream, events between them)
+    e[0].record()
+    rot, mu = _rotations(x, F, A, Ap, dref, _lib.MODE_CENTER, want_mu=True)
+    e[1].record()
+    _lib.check(lib.gbrmsd_apply_rotations(x.data_ptr(), F, A, 3 * Ap, rot.data_ptr(), mu.data_ptr(), off, None,
+                                          stream))
+    e[2].record()
+    torch.cuda.synchronize()
+    ms_rot, ms_apply = e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2])
+    alg = 36.0 * A * F  # rotation pass reads 12 B/atom; the apply pass reads and writes 12 B/atom
+    peaks = measured_peaks()
+    ach = alg / (ms_step / 1e3) / 1e9
+    roof = {"bound": "hbm", "achieved": round(ach, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
+            "frac": round(ach / peaks["hbm_gbs"], 4), "traffic": None,
+            "kernel": "stream_kernel + finish_kernel + apply_rotations_kernel (whole step)",
+            "algorithmic_bytes_per_step": alg,
+            "passes_ms": {"rotations": round(ms_rot, 4), "apply": round(ms_apply, 4)},
+            "apply_GBs": round(24.0 * A * F / (ms_apply / 1e3) / 1e9, 1),
+            "rotations_GBs": round(12.0 * A * F / (ms_rot / 1e3) / 1e9, 1), "peak_src": peaks["src"]}
+    # rmsf on the device-resident frames: centring + rotations + reduction
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    traces = D.center_inplace(x, F, A, Ap, _lib.ATOM_MAJOR)
+    rf = x.view(F, Ap, 3)[0, :A].cpu().numpy()
+    rref = D.DeviceReference(rf, _lib.ATOM_MAJOR, centre=False, device=dev)
+    rws = D.empty_bytes(lib.gbrmsd_rmsf_workspace_bytes(F, A), dev)
+    rout = torch.empty(A, dtype=torch.float32, device=dev)
+
+    def rmsf_step():
+        tr = D.center_inplace(x, F, A, Ap, _lib.ATOM_MAJOR, traces_out=traces)
+        rot2, _ = _rotations(x, F, A, Ap, rref, _lib.MODE_PRECENTERED, tr, float(np.float32((rf ** 2).sum())))
+        _lib.check(lib.gbrmsd_rmsf(x.data_ptr(), F, A, 3 * Ap, rot2.data_ptr(), rout.data_ptr(), rws.data_ptr(),
+                                   rws.numel(), stream))
+
+    rmsf_step()
+    torch.cuda.synchronize()
+    t0.record()
+    for _ in range(args.steps):
+        rmsf_step()
+    t1.record()
+    torch.cuda.synchronize()
+    ms_rmsf = t0.elapsed_time(t1) / args.steps
+    rmsf_sec = {"ms_per_call": round(ms_rmsf, 4), "frames_per_s": round(F / (ms_rmsf / 1e3), 1),
+                "algorithmic_bytes": 48.0 * A * F,
+                "achieved_GBs": round(48.0 * A * F / (ms_rmsf / 1e3) / 1e9, 1),
+                "note": "centring in place (read + write), rotation pass, rotated reduction (12 B/atom each read)"}
+    e2e = None
+    if rank == 0 and not args.skip_e2e:
+        host = np.empty((F, A, 3), dtype=np.float32)
+        D.frames_to_host(x, host, _lib.ATOM_MAJOR, A, Ap, stream)
+        torch.cuda.synchronize()
+        traj = md.Trajectory(host)
+        traj.superpose(traj, 0)
+        reps = max(1, min(3, args.steps))
+        t_e = time.perf_counter()
+        for _ in range(reps):
+            traj.superpose(traj, 0)
+        dt = (time.perf_counter() - t_e) / reps
+        e2e = {"value": round(F / dt, 1), "unit": "frames/s", "h2d_bytes_per_step": 12 * A * F,
+               "d2h_bytes_per_step": 12 * A * F, "note": "Trajectory.superpose on a host numpy array"}
+        del host, traj
+    cpu_base = None
+    if rank == 0 and world == 1 and not args.skip_cpu:
+        from oracle import cpu
+
+        impl = cpu.CpuRmsd("reference")
+        n = min(F, 20000)
+        xs = np.ascontiguousarray(before[: min(len(before), n)])
+        xs = np.ascontiguousarray(np.concatenate([xs] * max(1, n // len(xs)))[:n])
+        t_c = time.perf_counter()
+        reps = 0
+        while True:
+            y = xs.copy()
+            impl.superpose(y, frame0)
+            reps += 1
+            if time.perf_counter() - t_c > args.cpu_budget or reps >= 20:
+                break
+        dt = (time.perf_counter() - t_c) / reps
+        cpu_base = {"value": round(n / dt, 1), "unit": "frames/s", "cores": cpu.n_threads(), "kind": "reference",
+                    "sample": "Trajectory.superpose of %d frames x %d atoms (numpy steps + the reference's compiled "
+                              "rotation loop), %d repetitions" % (n, A, reps)}
+    return {
+        "metric": "superpose_frames_per_s", "value": round(world * F / (ms_step / 1e3), 1), "unit": "frames/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded, generated on device)",
+        "config": {"workload": args.workload, "n_frames": F, "n_atoms": A, "sigma_nm": sig,
+                   "l2": "frames (%.1f GB) larger than L2; no flush" % (12.0 * A * F / 1e9)},
+        "roofline": roof, "rmsf": rmsf_sec,
+        "accuracy": {"checked_frames": int(len(sample)), "max_err_nm": float(err.max()),
+                     "rms_err_nm": float(np.sqrt((err ** 2).mean())), "oracle": "FP64 superposition (oracle/fp64.py)"},
+        "cpu_baseline": cpu_base, "e2e": e2e, "gpu_launches": 4 * args.steps, "clocks": clk.summary(),
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -978,6 +1138,8 @@ def main():
         res = run_ragged(args)
     elif args.workload.startswith("serving"):
         res = run_serving(args)
+    elif args.workload.startswith("superpose"):
+        res = run_superpose(args)
     else:
         res = run_gpu(args)
     rank = int(os.environ.get("RANK", "0"))

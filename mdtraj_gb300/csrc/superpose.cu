@@ -32,43 +32,76 @@ namespace {
 // of GB300's slow FP64 pipe.
 __device__ __forceinline__ float add_split(float x, float hi, float lo) { return (x + hi) + lo; }
 
-constexpr int APPLY_THREADS = 256;
+constexpr int APPLY_THREADS = 128;
 
+// Per-frame constants of the apply pass: R and -mu split into float hi + lo.
+struct ApplyFrame {
+  float r[9];
+  float mh[3], ml[3];
+};
+
+__device__ __forceinline__ void apply_one(const ApplyFrame& p, const float (&oh)[3], const float (&ol)[3], float& x,
+                                          float& y, float& z, bool& nz) {
+  const float dx = add_split(x, p.mh[0], p.ml[0]);
+  const float dy = add_split(y, p.mh[1], p.ml[1]);
+  const float dz = add_split(z, p.mh[2], p.ml[2]);
+  const float rx = fmaf(p.r[0], dx, fmaf(p.r[1], dy, p.r[2] * dz));
+  const float ry = fmaf(p.r[3], dx, fmaf(p.r[4], dy, p.r[5] * dz));
+  const float rz = fmaf(p.r[6], dx, fmaf(p.r[7], dy, p.r[8] * dz));
+  nz = nz || (rx != 0.f) || (ry != 0.f) || (rz != 0.f);
+  x = add_split(rx, oh[0], ol[0]);
+  y = add_split(ry, oh[1], ol[1]);
+  z = add_split(rz, oh[2], ol[2]);
+}
+
+// One CTA per (frame, block of 4 * APPLY_THREADS atoms); each thread moves one
+// 4-atom quad with three 128-bit loads and stores when the frame is 16-byte
+// aligned (VEC), else atom by atom.
+template <bool VEC>
 __global__ void __launch_bounds__(APPLY_THREADS) apply_rotations_kernel(float* __restrict__ x, int64_t F, int32_t A,
                                                                        int64_t fs, const float* __restrict__ rot,
-                                                                       const double* __restrict__ mu, double o0,
-                                                                       double o1, double o2, int32_t* nonzero0) {
-  const int32_t nab = (A + APPLY_THREADS - 1) / APPLY_THREADS;
+                                                                       const double* __restrict__ mu, float oh0,
+                                                                       float oh1, float oh2, float ol0, float ol1,
+                                                                       float ol2, int32_t* nonzero0) {
+  __shared__ ApplyFrame sp;
+  constexpr int ATOMS_PER_CTA = 4 * APPLY_THREADS;
+  const int32_t nab = (A + ATOMS_PER_CTA - 1) / ATOMS_PER_CTA;
   const int64_t f = blockIdx.x / nab;
-  const int32_t k = (int32_t)(blockIdx.x - f * nab) * APPLY_THREADS + threadIdx.x;
-  if (f >= F) return;
-  float r[9];
-#pragma unroll
-  for (int i = 0; i < 9; ++i) r[i] = rot[9 * f + i];
-  float mh[3] = {0.f, 0.f, 0.f}, ml[3] = {0.f, 0.f, 0.f};
-  if (mu) {
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      const double m = mu[3 * f + c];
-      mh[c] = -(float)m;
-      ml[c] = -(float)(m + (double)mh[c]);
-    }
+  const int32_t k0 = (int32_t)(blockIdx.x - f * nab) * ATOMS_PER_CTA;
+  if (threadIdx.x < 9) sp.r[threadIdx.x] = rot[9 * f + threadIdx.x];
+  if (threadIdx.x >= 16 && threadIdx.x < 19) {
+    const int c = threadIdx.x - 16;
+    const double m = mu ? mu[3 * f + c] : 0.0;
+    const float hi = -(float)m;
+    sp.mh[c] = hi;
+    sp.ml[c] = -(float)(m + (double)hi);
   }
-  const float oh[3] = {(float)o0, (float)o1, (float)o2};
-  const float ol[3] = {(float)(o0 - (double)oh[0]), (float)(o1 - (double)oh[1]), (float)(o2 - (double)oh[2])};
+  __syncthreads();
+  const float oh[3] = {oh0, oh1, oh2}, ol[3] = {ol0, ol1, ol2};
   bool nz = false;
-  if (k < A) {
-    float* p = x + f * fs + 3 * (int64_t)k;
-    const float dx = add_split(p[0], mh[0], ml[0]);
-    const float dy = add_split(p[1], mh[1], ml[1]);
-    const float dz = add_split(p[2], mh[2], ml[2]);
-    const float rx = fmaf(r[0], dx, fmaf(r[1], dy, r[2] * dz));
-    const float ry = fmaf(r[3], dx, fmaf(r[4], dy, r[5] * dz));
-    const float rz = fmaf(r[6], dx, fmaf(r[7], dy, r[8] * dz));
-    nz = (rx != 0.f) || (ry != 0.f) || (rz != 0.f);
-    p[0] = add_split(rx, oh[0], ol[0]);
-    p[1] = add_split(ry, oh[1], ol[1]);
-    p[2] = add_split(rz, oh[2], ol[2]);
+  float* fr = x + f * fs;
+  const int32_t k = k0 + 4 * threadIdx.x;
+  if (VEC && k + 3 < A) {
+    float4* q = reinterpret_cast<float4*>(fr + 3 * (int64_t)k);
+    float4 a = q[0], b = q[1], c = q[2];
+    apply_one(sp, oh, ol, a.x, a.y, a.z, nz);
+    apply_one(sp, oh, ol, a.w, b.x, b.y, nz);
+    apply_one(sp, oh, ol, b.z, b.w, c.x, nz);
+    apply_one(sp, oh, ol, c.y, c.z, c.w, nz);
+    q[0] = a;
+    q[1] = b;
+    q[2] = c;
+  } else {
+    for (int t = 0; t < 4; ++t) {
+      if (k + t < A) {
+        float* p = fr + 3 * (int64_t)(k + t);
+        float px = p[0], py = p[1], pz = p[2];
+        apply_one(sp, oh, ol, px, py, pz, nz);
+        p[0] = px;
+        p[1] = py;
+        p[2] = pz;
+      }
+    }
   }
   if (nonzero0 && f == 0 && __any_sync(FULL_MASK, nz) && (threadIdx.x & 31) == 0) atomicOr(nonzero0, 1);
 }
@@ -230,11 +263,22 @@ int gbrmsd_apply_rotations(float* x, int64_t n_frames, int32_t n_atoms, int64_t 
   if (nonzero0) GB_CUDA_TRY(cudaMemsetAsync(nonzero0, 0, sizeof(int32_t), st), "memset nonzero flag");
   if (n_frames == 0 || n_atoms == 0) return GBRMSD_OK;
   if (!rot) return set_error(GBRMSD_E_INVALID, "apply_rotations: null rotations");
-  const int64_t nab = (n_atoms + APPLY_THREADS - 1) / APPLY_THREADS;
+  const int64_t nab = (n_atoms + 4 * APPLY_THREADS - 1) / (4 * APPLY_THREADS);
   if (n_frames * nab > 0x7fffffffLL) return set_error(GBRMSD_E_INVALID, "apply_rotations: too many frames");
-  const double o0 = offset3 ? offset3[0] : 0.0, o1 = offset3 ? offset3[1] : 0.0, o2 = offset3 ? offset3[2] : 0.0;
-  apply_rotations_kernel<<<(unsigned)(n_frames * nab), APPLY_THREADS, 0, st>>>(x, n_frames, n_atoms, frame_stride, rot,
-                                                                               centroids, o0, o1, o2, nonzero0);
+  float oh[3], ol[3];
+  for (int c = 0; c < 3; ++c) {
+    const double o = offset3 ? offset3[c] : 0.0;
+    oh[c] = (float)o;
+    ol[c] = (float)(o - (double)oh[c]);
+  }
+  const bool vec = aligned16(x) && (frame_stride % 4) == 0;
+  const unsigned grid = (unsigned)(n_frames * nab);
+  if (vec)
+    apply_rotations_kernel<true><<<grid, APPLY_THREADS, 0, st>>>(x, n_frames, n_atoms, frame_stride, rot, centroids,
+                                                                 oh[0], oh[1], oh[2], ol[0], ol[1], ol[2], nonzero0);
+  else
+    apply_rotations_kernel<false><<<grid, APPLY_THREADS, 0, st>>>(x, n_frames, n_atoms, frame_stride, rot, centroids,
+                                                                  oh[0], oh[1], oh[2], ol[0], ol[1], ol[2], nonzero0);
   GB_CUDA_TRY(cudaGetLastError(), "launch apply_rotations_kernel");
   return GBRMSD_OK;
 }

@@ -66,6 +66,8 @@ class CpuRmsd:
             self.lib = _load(REF_SO, "ref")
             self.prefix = "ref"
             self.lib.ref_center_inplace.argtypes = [_vp, _i64, _i32, _vp]
+            self.lib.ref_superpose_atom_major.argtypes = [_vp, _vp, C.c_float, _vp, _vp, _i64, _i32, _i32]
+            self.lib.ref_rmsf_rotated.argtypes = [_vp, _vp, C.c_float, _vp, _vp, _i64, _i32, _i32, _vp]
         else:
             raise ValueError(kind)
 
@@ -100,6 +102,39 @@ class CpuRmsd:
         out = np.empty(target.shape[0], dtype=np.float32)
         self.lib.port_nosuperpose(target.ctypes.data, target.shape[0], target.shape[1], ref_frame.ctypes.data,
                                   out.ctypes.data)
+        return out
+
+
+    def superpose(self, xyz: np.ndarray, ref_frame: np.ndarray) -> None:
+        """Trajectory.superpose(t, ref, frame) on all atoms, in place on xyz
+        (float32 C (F, A, 3)): the numpy steps of core/trajectory.py:1124-1165
+        around the reference's compiled rotation loop."""
+        if self.kind != "reference":
+            raise NotImplementedError("superpose needs the reference's rotation kernels")
+        n = xyz.shape[0]
+        offset = np.mean(xyz, axis=1, dtype=np.float64).reshape(n, 1, 3)
+        xyz -= offset
+        ref_align = np.array(ref_frame, dtype=np.float32, copy=True, order="C").reshape(1, -1, 3)
+        ref_offset = ref_align[0].astype(np.float64).mean(0)
+        ref_align[0] -= ref_offset
+        g = np.einsum("ijk,ijk->i", xyz, xyz)
+        ref_g = np.einsum("ijk,ijk->i", ref_align, ref_align)
+        self.lib.ref_superpose_atom_major(ref_align.ctypes.data, xyz.ctypes.data, float(ref_g[0]), g.ctypes.data,
+                                          xyz.ctypes.data, n, xyz.shape[1], xyz.shape[1])
+        xyz += ref_offset
+
+    def rmsf(self, xyz: np.ndarray, ref_frame: np.ndarray) -> np.ndarray:
+        """rmsf(t, ref, frame) on all atoms (_rmsd.pyx:389-456): centres xyz
+        and a copy of the reference frame in place, rotates a copy, reduces."""
+        if self.kind != "reference":
+            raise NotImplementedError("rmsf needs the reference's rotation kernels")
+        g = self.center_inplace(xyz)
+        r = np.array(ref_frame, dtype=np.float32, copy=True, order="C").reshape(1, -1, 3)
+        rg = self.center_inplace(r)
+        disp = xyz.copy()
+        out = np.empty(xyz.shape[1], dtype=np.float32)
+        self.lib.ref_rmsf_rotated(xyz.ctypes.data, r.ctypes.data, float(rg[0]), g.ctypes.data, disp.ctypes.data,
+                                  xyz.shape[0], xyz.shape[1], 1, out.ctypes.data)
         return out
 
 

@@ -92,3 +92,22 @@ def test_fp64_superpose_rmsf_align_displace_match_reference(golden):
     assert np.abs(d - g["ad_rmsd"]).max() < 2e-5
     # the reference's rotation array equals R (frame aligned onto the reference frame)
     assert np.abs(R - g["ad_rot"]).max() < 2e-5
+
+
+def test_reference_superpose_and_rmsf_drivers_match_fixture(golden):
+    """oracle/ref_driver.cpp's replay of superpose_atom_major and rmsf over the
+    reference's compiled kernels (the CPU baseline of the superpose workload)
+    reproduces the reference's Cython outputs."""
+    from oracle import cpu
+
+    try:
+        ref = cpu.CpuRmsd("reference")
+    except (FileNotFoundError, OSError):
+        pytest.skip("reference sources not available")
+    g = golden("superpose_rmsf.npz")
+    x = g["xyz"]
+    y = x.copy()
+    ref.superpose(y, x[3])
+    np.testing.assert_array_equal(y, g["sup_all_f3"])
+    y = x.copy()
+    assert np.abs(ref.rmsf(y, x[0]) - g["rmsf_self_f0"]).max() < 1e-5
