@@ -179,6 +179,27 @@ int gbrmsd_rmsf(const float* x, int64_t n_frames, int32_t n_atoms, int64_t frame
 int gbrmsd_rotated_rmsd(const float* x, int64_t n_frames, int32_t n_atoms, int64_t frame_stride, const float* rot,
                         const float* ref_frame, float* out_rmsd, void* stream);
 
+/* ---- XTC trajectories decoded on the GPU -----------------------------------
+ * Replaces the reference's XTC reader (formats/xtc/xtc.pyx over
+ * xdrfile_xtc.c:38-87 and the coordinate decompression of xdrfile.c:779-998)
+ * for feeding frames to the RMSD kernels without a host decode.
+ * gbrmsd_xtc_index (host only): scans the XDR frame headers of `data`
+ * (nbytes of an XTC file or of a chunk of one starting at a frame boundary),
+ * writes up to `capacity` frame byte offsets, the number of complete frames,
+ * their atom count (all frames must match) and the bytes they span
+ * (`consumed`; a truncated last frame is left out).
+ * gbrmsd_xtc_decode: one thread per frame decodes `data` (device copy) at the
+ * given offsets (device) into xyz (device, atom-major, frame_stride floats per
+ * frame), with optional step / time / box (9 floats) per frame and a status
+ * per frame (0 ok; 1 bad magic, 2 atom count, 3 truncated or overrun, 4 bad
+ * small-integer index).  Coordinates equal the reference reader's: integer
+ * coordinate times float(1 / precision), in float. */
+int gbrmsd_xtc_index(const uint8_t* data, int64_t nbytes, int64_t* offsets, int64_t capacity, int64_t* n_frames,
+                     int32_t* n_atoms, int64_t* consumed);
+int gbrmsd_xtc_decode(const uint8_t* data, int64_t nbytes, const int64_t* offsets, int64_t n_frames, int32_t n_atoms,
+                      float* xyz, int64_t frame_stride, int32_t* step, float* time, float* box, int32_t* status,
+                      void* stream);
+
 /* ---- Cross RMSD: query frames against a resident database ------------------
  * Replaces `[md.rmsd(db[a:b], queries, k, precentered=True) for k in ...]`
  * (_rmsd.pyx:64-243 per query frame) for many requests at once.  A frame set

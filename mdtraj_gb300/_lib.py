@@ -59,6 +59,8 @@ SIGNATURES: dict[str, tuple] = {
     "gbrmsd_rmsf_workspace_bytes": (_sz, [_i64, _i32]),
     "gbrmsd_rmsf": (C.c_int, [_vp, _i64, _i32, _i64, _vp, _vp, _vp, _sz, _vp]),
     "gbrmsd_rotated_rmsd": (C.c_int, [_vp, _i64, _i32, _i64, _vp, _vp, _vp, _vp]),
+    "gbrmsd_xtc_index": (C.c_int, [_vp, _i64, _vp, _i64, _vp, _vp, _vp]),
+    "gbrmsd_xtc_decode": (C.c_int, [_vp, _i64, _vp, _i64, _i32, _vp, _i64, _vp, _vp, _vp, _vp, _vp]),
     "gbrmsd_frameset_bytes": (_sz, [_i64, _i32]),
     "gbrmsd_frameset_prepare": (C.c_int, [_vp, _i64, _i32, _i32, _i64, _i32, _i32, _vp, _i64, _i64, _vp]),
     "gbrmsd_cross_workspace_bytes": (_sz, [_i64, _i64, _i32]),

@@ -149,3 +149,27 @@ def best_available() -> CpuRmsd:
 def n_threads() -> int:
     v = os.environ.get("OMP_NUM_THREADS")
     return int(v) if v else (os.cpu_count() or 1)
+
+
+XTC_SO = HERE / "_ref" / platform.machine() / "libref_xtc.so"
+
+
+def read_xtc_reference(path, n_atoms: int, max_frames: int):
+    """(xyz (F, A, 3), step, time, box (F, 3, 3)) read by the reference's C XTC
+    reader (oracle/ref_xtc_driver.c)."""
+    if not XTC_SO.exists():
+        build(ref=True)
+    if not XTC_SO.exists():
+        raise FileNotFoundError("reference XTC reader could not be built (no sources)")
+    lib = C.CDLL(str(XTC_SO))
+    lib.ref_xtc_read.restype = C.c_int
+    lib.ref_xtc_read.argtypes = [C.c_char_p, C.c_int, C.c_long, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    xyz = np.zeros((max_frames, n_atoms, 3), np.float32)
+    step = np.zeros(max_frames, np.int32)
+    time = np.zeros(max_frames, np.float32)
+    box = np.zeros((max_frames, 3, 3), np.float32)
+    n = lib.ref_xtc_read(str(path).encode(), n_atoms, max_frames, xyz.ctypes.data, step.ctypes.data,
+                         time.ctypes.data, box.ctypes.data)
+    if n < 0:
+        raise FileNotFoundError(str(path))
+    return xyz[:n], step[:n], time[:n], box[:n]

@@ -24,6 +24,9 @@ through a stub ``mdtraj`` package, and records:
                     with the in-place centring side effects) and
                     getMultipleAlignDisplaceRMSDs_atom_major (distances and
                     rotation matrices), all from the reference.
+* xtc_{water,tiny,wide}.xtc + xtc_cases.npz — synthetic trajectories written
+                    by the reference's XTC writer, with its reader's output
+                    (coordinates, time, step, box) for the GPU decoder.
 
 Usage:  python tests/golden/make_golden.py
 """
@@ -294,6 +297,41 @@ def superpose_fixture(_rmsd) -> None:
     np.savez_compressed(OUT / "superpose_rmsf.npz", **arrays)
 
 
+def xtc_fixture(xtc) -> None:
+    """xtc_*.xtc + xtc_cases.npz: synthetic trajectories written by the
+    reference's XTC writer and read back by its reader (formats/xtc), for the
+    GPU decoder.  Cases: 'water' (333 three-atom clusters + 2 atoms: runs of
+    small integer differences), 'tiny' (7 atoms: stored uncompressed),
+    'wide' (coordinates spanning 18,000 nm: per-dimension integer sizes)."""
+    rng = np.random.default_rng(41)
+    cases = {}
+    centres = rng.uniform(0, 5, size=(333, 1, 3))
+    offsets = rng.normal(0, 0.08, size=(333, 3, 3))
+    base = np.concatenate([(centres + offsets).reshape(-1, 3), rng.uniform(0, 5, size=(2, 3))])
+    cases["water"] = base[None] + rng.normal(0, 0.02, size=(40, len(base), 3))
+    cases["tiny"] = rng.uniform(-1, 1, size=(12, 7, 3))
+    wide = rng.uniform(-1, 1, size=(5, 50, 3))
+    wide[:, :, 0] *= 9000.0
+    cases["wide"] = wide
+    arrays = {}
+    for name, x in cases.items():
+        x = x.astype(np.float32)
+        n = len(x)
+        path = OUT / f"xtc_{name}.xtc"
+        time = (np.arange(n) * 2.5 + 10).astype(np.float32)
+        step = (np.arange(n) * 1000 + 7).astype(np.int32)
+        box = np.repeat((np.eye(3) * np.float32(5.5 + 0.1 * len(name)))[None], n, 0).astype(np.float32)
+        with xtc.XTCTrajectoryFile(str(path), "w") as f:
+            f.write(x, time=time, step=step, box=box)
+        with xtc.XTCTrajectoryFile(str(path)) as f:
+            xyz, t, st, bx = f.read()
+        arrays[f"{name}__xyz"] = np.asarray(xyz, dtype=np.float32)
+        arrays[f"{name}__time"] = np.asarray(t, dtype=np.float32)
+        arrays[f"{name}__step"] = np.asarray(st, dtype=np.int32)
+        arrays[f"{name}__box"] = np.asarray(bx, dtype=np.float32)
+    np.savez_compressed(OUT / "xtc_cases.npz", **arrays)
+
+
 def main() -> None:
     build_reference_python()
     _rmsd, xtc = import_reference()
@@ -301,6 +339,7 @@ def main() -> None:
     alignment_fixture()
     synthetic_fixture(_rmsd)
     superpose_fixture(_rmsd)
+    xtc_fixture(xtc)
     for p in sorted(OUT.glob("*.npz")):
         print(p.name, p.stat().st_size, "bytes")
 

@@ -111,3 +111,24 @@ def test_reference_superpose_and_rmsf_drivers_match_fixture(golden):
     np.testing.assert_array_equal(y, g["sup_all_f3"])
     y = x.copy()
     assert np.abs(ref.rmsf(y, x[0]) - g["rmsf_self_f0"]).max() < 1e-5
+
+
+def test_reference_c_xtc_reader_matches_fixture(golden):
+    """The reference's C XTC reader (the CPU baseline of the decoding workload)
+    returns what the reference's Cython reader returned for the fixtures."""
+    from pathlib import Path
+
+    from oracle import cpu
+
+    g = golden("xtc_cases.npz")
+    for name in ("water", "tiny", "wide"):
+        want = g[f"{name}__xyz"]
+        try:
+            xyz, step, time, box = cpu.read_xtc_reference(Path(__file__).parent / "golden" / f"xtc_{name}.xtc",
+                                                         want.shape[1], 1000)
+        except FileNotFoundError:
+            pytest.skip("reference XTC sources not available")
+        np.testing.assert_array_equal(xyz, want)
+        np.testing.assert_array_equal(step, g[f"{name}__step"])
+        np.testing.assert_array_equal(time, g[f"{name}__time"])
+        np.testing.assert_array_equal(box, g[f"{name}__box"])
