@@ -1,32 +1,38 @@
-// All-pairs RMSD on the 5th-generation tensor cores (tcgen05, sm_103a).
+// All-pairs and cross RMSD on the 5th-generation tensor cores (tcgen05, sm_103a).
 //
-// P = X X^T with X = hi + lo split into two BF16 planes, computed as
-// hi.hi^T + hi.lo^T + lo.hi^T with FP32 accumulation in tensor memory
-// (the lo.lo^T term is ~2^-18 relative and dropped).  One tile is a
-// 128 x 240 block of P: 42 frames (126 rows + 2 ignored) by 80 frames.
+// P = X Y^T with each operand split into two BF16 planes (hi + lo), computed
+// as hi.hi^T + hi.lo^T + lo.hi^T with FP32 accumulation in tensor memory (the
+// lo.lo^T term is ~2^-18 relative and dropped).  One tile is a 128 x 240 block
+// of P: 42 row frames (126 rows + 2 ignored) by 80 column frames.
 //
 // The tensor core's FP32 accumulator loses a fraction of an ulp per add in
 // one direction; over the 384 accumulation steps of a 2,048-atom tile that
-// biases msd by ~1e-4 nm^2.  Each 64-atom k block therefore accumulates into
-// a fresh TMEM buffer (12 MMAs), and CUDA-core warps fold the buffer into FP32
-// registers with round-to-nearest adds (the promotion of partial sums used for
-// low-precision tensor GEMMs), which shrinks the bias ~32-fold.
+// biases msd by ~1e-4 nm^2.  The MMAs therefore accumulate only KFOLD k blocks
+// (2 x 64 atoms, 24 steps) into the partial buffer P in tensor memory, and
+// CUDA-core warps fold P into FP32 registers with round-to-nearest adds (the
+// promotion of partial sums used for low-precision tensor GEMMs).
 //
 // Persistent CTAs (one per SM), 448 threads:
 //   warp 0       TMA producer: per 64-atom k block, four 2-D tensor copies
 //                (A_hi, A_lo 128 x 64; B_hi, B_lo 240 x 64; 128-byte swizzle)
 //                into a 2-stage shared-memory ring;
-//   warp 1       allocates 512 TMEM columns (two 240-column k-block
-//                buffers); one lane issues 12 tcgen05.mma per k block (3
-//                products x 4 k-steps of 16) and commits the stage release and
-//                the buffer-full signal to mbarriers;
-//   warps 2..13  accumulators + epilogue: warp w owns TMEM lanes 32*(w%4).. and
-//                80 of the 240 columns; it folds every k-block buffer into 80
-//                registers, then stages the tile in 48-column chunks (16
-//                frames) through shared memory, solves QCP per pair in FP32
-//                (allpairs.cuh) and writes both triangles.
-// Every wait is bounded; on a timeout the thread records an error and leaves
-// its loop, and the CTA frees its tensor memory before exiting.
+//   warp 1       allocates 512 TMEM columns -- P (columns 0-239) and the
+//                result buffer R (256-495) -- and one lane issues the MMAs:
+//                12 tcgen05.mma per k block (3 products x 4 k-steps of 16),
+//                committing each stage's release and each fold unit's
+//                completion to mbarriers;
+//   warps 2..13  workers: warp w owns TMEM lanes 32*(w%4).. and 80 of the 240
+//                columns.  For every fold unit of tile t they add P into 80
+//                registers, release P, and then run one pass of the epilogue of
+//                tile t-1, which waits in R: a pass stages a 48-column chunk of
+//                R in shared memory (first pass of a chunk) and solves QCP in
+//                FP32 (allpairs.cuh) for up to 384 of the chunk's 672 frame
+//                pairs.  At the end of tile t (after finishing tile t-1's
+//                passes) they store their registers into R.  So the epilogue
+//                of one tile runs while the tensor cores work on the next.
+// Every wait is bounded; the workers agree on a failure at every fold unit
+// (barrier with an OR reduction) so that no named barrier can be left half
+// entered; the CTA frees its tensor memory before exiting.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <string.h>
@@ -45,6 +51,7 @@ constexpr int TILE_N = 240;             // columns of P per tile (tensor-core N)
 constexpr int FR_M = 42;                // frames per tile row block (126 rows)
 constexpr int FR_N = 80;                // frames per tile column block
 constexpr int KBLK = 64;                // atoms per k block (128 B of BF16 = one swizzle row)
+constexpr int KFOLD = 2;                // k blocks accumulated in P per fold
 constexpr int NSTAGE = 2;
 constexpr int A_BYTES = TILE_M * KBLK * 2;  // 16 KB
 constexpr int B_BYTES = TILE_N * KBLK * 2;  // 30 KB
@@ -52,14 +59,21 @@ constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
 constexpr int EPI_COLS = 48;            // 16 frames per epilogue chunk
 constexpr int EPI_LD = EPI_COLS + 1;
 constexpr int EPI_BYTES = TILE_M * EPI_LD * 4;
+constexpr int NCHUNK = TILE_N / EPI_COLS;       // 5 chunks per tile
+constexpr int CHUNK_PAIRS = FR_M * 16;          // 672 frame pairs per chunk
 constexpr int TMEM_COLS = 512;
-constexpr int ACC_STRIDE = 256;         // TMEM columns between the two k-block buffers
+constexpr uint32_t P_COL = 0;           // partial (fold) buffer
+constexpr uint32_t R_COL = 256;         // result buffer of the tile awaiting its epilogue
 constexpr int NGROUP = 3;               // column groups per TMEM lane slice
 constexpr int GCOLS = TILE_N / NGROUP;  // 80 accumulator registers per thread
-constexpr int NEPI = 4 * NGROUP;        // accumulator / epilogue warps
+constexpr int NEPI = 4 * NGROUP;        // worker warps
 constexpr int NEPI_THREADS = 32 * NEPI;
 constexpr int NTHREADS = 64 + NEPI_THREADS;
+constexpr int PASSES_PER_CHUNK = (CHUNK_PAIRS + NEPI_THREADS - 1) / NEPI_THREADS;  // 2
+constexpr int PASSES = NCHUNK * PASSES_PER_CHUNK;                                 // 10 per tile
 constexpr uint32_t SPIN = 1u << 24;
+static_assert(EPI_COLS == NGROUP * 16, "one 16-column TMEM load per worker warp per chunk");
+static_assert(R_COL + TILE_N <= TMEM_COLS && P_COL + TILE_N <= R_COL, "TMEM layout");
 
 // smem: [stages | epilogue staging | barriers | tmem address | cross column views]
 constexpr int SMEM_STAGES = NSTAGE * STAGE_BYTES;
@@ -169,36 +183,32 @@ __device__ __forceinline__ bool wait_bar(uint64_t* bar, uint32_t parity, int* er
   return mbar_wait_bounded(bar, parity, err, SPIN);
 }
 
-// Epilogue staging: accumulator column q of column group G goes to staging
-// column q - lo of chunk C (lo = 48 C - 80 G) when it falls inside the chunk.
-// One instantiation per (G, C) so that the column ranges are compile-time.
-template <int G, int C>
-__device__ __forceinline__ void stage_chunk_t(float* dst, const float (&acc)[GCOLS]) {
-  constexpr int lo = C * EPI_COLS - G * GCOLS;
-#pragma unroll
-  for (int q = 0; q < GCOLS; ++q)
-    if (q - lo >= 0 && q - lo < EPI_COLS) dst[q - lo] = acc[q];
+__device__ __forceinline__ void tc_st16(uint32_t taddr, const float (&v)[16]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15, %16};" ::"r"(taddr),
+      "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])), "r"(__float_as_uint(v[3])),
+      "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])), "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])),
+      "r"(__float_as_uint(v[8])), "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])),
+      "r"(__float_as_uint(v[11])), "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])),
+      "r"(__float_as_uint(v[14])), "r"(__float_as_uint(v[15]))
+      : "memory");
 }
+__device__ __forceinline__ void tc_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
-__device__ __forceinline__ void stage_chunk(int gc, float* dst, const float (&acc)[GCOLS]) {
-  static_assert(NGROUP == 3 && TILE_N / EPI_COLS == 5, "staging cases");
-  switch (gc) {
-    case 0: stage_chunk_t<0, 0>(dst, acc); break;
-    case 1: stage_chunk_t<0, 1>(dst, acc); break;
-    case 2: stage_chunk_t<0, 2>(dst, acc); break;
-    case 3: stage_chunk_t<0, 3>(dst, acc); break;
-    case 4: stage_chunk_t<0, 4>(dst, acc); break;
-    case 5: stage_chunk_t<1, 0>(dst, acc); break;
-    case 6: stage_chunk_t<1, 1>(dst, acc); break;
-    case 7: stage_chunk_t<1, 2>(dst, acc); break;
-    case 8: stage_chunk_t<1, 3>(dst, acc); break;
-    case 9: stage_chunk_t<1, 4>(dst, acc); break;
-    case 10: stage_chunk_t<2, 0>(dst, acc); break;
-    case 11: stage_chunk_t<2, 1>(dst, acc); break;
-    case 12: stage_chunk_t<2, 2>(dst, acc); break;
-    case 13: stage_chunk_t<2, 3>(dst, acc); break;
-    default: stage_chunk_t<2, 4>(dst, acc); break;
-  }
+// Named barrier that also ORs a flag over its n threads: every thread gets the
+// same answer, so a decision taken on it cannot split the group.
+__device__ __forceinline__ bool named_bar_or(int id, int n, bool v) {
+  int r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "setp.ne.b32 q, %1, 0;\n\t"
+      "bar.red.or.pred p, %2, %3, q;\n\t"
+      "selp.b32 %0, 1, 0, p;\n\t}"
+      : "=r"(r)
+      : "r"((int)v), "r"(id), "r"(n)
+      : "memory");
+  return r != 0;
 }
 
 template <bool CROSS>
@@ -214,9 +224,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) allpairs_tc_kernel(const __grid_c
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + SMEM_BAR);
   uint64_t* full = bars;                  // [NSTAGE] operands landed
   uint64_t* empty = bars + NSTAGE;        // [NSTAGE] operands consumed by the MMAs
-  uint64_t* kfull = bars + 2 * NSTAGE;    // [2] k-block buffer written
-  uint64_t* kempty = kfull + 2;           // [2] k-block buffer folded by all accumulator warps
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(kempty + 2);
+  uint64_t* pfull = bars + 2 * NSTAGE;    // P holds a finished fold unit
+  uint64_t* pempty = pfull + 1;           // P folded by all worker warps
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(pempty + 1);
   volatile int* fail_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
   CrossCol* colv = reinterpret_cast<CrossCol*>(smem + SMEM_COLV);
 
@@ -228,10 +238,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) allpairs_tc_kernel(const __grid_c
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    for (int b = 0; b < 2; ++b) {
-      mbar_init(&kfull[b], 1);
-      mbar_init(&kempty[b], NEPI);
-    }
+    mbar_init(pfull, 1);
+    mbar_init(pempty, NEPI);
     *fail_flag = 0;
     fence_mbar_init();
   }
@@ -246,6 +254,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) allpairs_tc_kernel(const __grid_c
 
   const int64_t n_tiles = args.n_tiles;
   const int nkb = args.kpad / KBLK;
+  const int nunit = (nkb + KFOLD - 1) / KFOLD;
 
   if (warp == 0) {
     // ---------------- TMA producer ----------------
@@ -258,7 +267,11 @@ __global__ void __launch_bounds__(NTHREADS, 1) allpairs_tc_kernel(const __grid_c
         for (int kb = 0; kb < nkb; ++kb, ++it) {
           const int s = it % NSTAGE;
           const uint32_t use = it / NSTAGE;
-          if (use > 0 && !wait_bar(&empty[s], (use - 1) & 1, args.err)) { ok = false; break; }
+          if ((use > 0 && !wait_bar(&empty[s], (use - 1) & 1, args.err)) || *fail_flag) {
+            *fail_flag = 1;
+            ok = false;
+            break;
+          }
           unsigned char* st = smem + s * STAGE_BYTES;
           mbar_arrive_expect_tx(&full[s], STAGE_BYTES);
           tma_load_2d(st, &map_hi_a, kb * KBLK, row_a, &full[s]);
@@ -267,42 +280,53 @@ __global__ void __launch_bounds__(NTHREADS, 1) allpairs_tc_kernel(const __grid_c
           tma_load_2d(st + 2 * A_BYTES + B_BYTES, &map_lo_b, kb * KBLK, row_b, &full[s]);
         }
       }
-      // the last use of every stage must be consumed before the CTA exits
+      // no copy may still be landing when the CTA exits
       for (uint32_t k = (it > NSTAGE ? it - NSTAGE : 0); k < it; ++k)
-        if (!wait_bar(&empty[k % NSTAGE], (k / NSTAGE) & 1, args.err)) break;
+        if (!wait_bar(&full[k % NSTAGE], (k / NSTAGE) & 1, args.err)) break;
     }
   } else if (warp == 1) {
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
       constexpr uint32_t idesc = make_idesc(TILE_M, TILE_N);
-      uint32_t it = 0;  // k blocks issued (= k-block buffers used)
+      const uint32_t d_tmem = tmem_base + P_COL;
+      uint32_t it = 0, unit = 0;  // k blocks issued, fold units committed
       bool ok = true;
       for (int64_t t = blockIdx.x; t < n_tiles && ok; t += gridDim.x) {
         for (int kb = 0; kb < nkb; ++kb, ++it) {
-          const int b = it & 1;
-          const uint32_t buse = it >> 1;
-          if (buse > 0 && !wait_bar(&kempty[b], (buse - 1) & 1, args.err)) { ok = false; break; }
+          const bool first = (kb % KFOLD) == 0;
+          if (first && unit > 0 && (!wait_bar(pempty, (unit - 1) & 1, args.err) || *fail_flag)) {
+            *fail_flag = 1;
+            ok = false;
+            break;
+          }
           const int s = it % NSTAGE;
-          if (!wait_bar(&full[s], (it / NSTAGE) & 1, args.err)) { ok = false; break; }
+          if (!wait_bar(&full[s], (it / NSTAGE) & 1, args.err)) {
+            *fail_flag = 1;
+            ok = false;
+            break;
+          }
           tc_fence_after();
-          const uint32_t d_tmem = tmem_base + b * ACC_STRIDE;
           const uint32_t st = smem_addr(smem + s * STAGE_BYTES);
           const uint32_t a_hi = st, a_lo = st + A_BYTES, b_hi = st + 2 * A_BYTES, b_lo = st + 2 * A_BYTES + B_BYTES;
 #pragma unroll
           for (int ks = 0; ks < KBLK / 16; ++ks) {
             const uint32_t koff = ks * 32;  // 16 BF16 = 32 bytes inside the 128-byte swizzle row
-            tc_mma(d_tmem, smem_desc_sw128(a_hi + koff), smem_desc_sw128(b_hi + koff), idesc, ks > 0 ? 1u : 0u);
+            tc_mma(d_tmem, smem_desc_sw128(a_hi + koff), smem_desc_sw128(b_hi + koff), idesc,
+                   (first && ks == 0) ? 0u : 1u);
             tc_mma(d_tmem, smem_desc_sw128(a_hi + koff), smem_desc_sw128(b_lo + koff), idesc, 1u);
             tc_mma(d_tmem, smem_desc_sw128(a_lo + koff), smem_desc_sw128(b_hi + koff), idesc, 1u);
           }
           tc_commit(&empty[s]);  // operand stage reusable once these MMAs have read it
-          tc_commit(&kfull[b]);  // k-block buffer ready for the accumulator warps
+          if ((kb % KFOLD) == KFOLD - 1 || kb == nkb - 1) {
+            tc_commit(pfull);    // fold unit complete in P
+            ++unit;
+          }
         }
       }
-      if (it > 0) wait_bar(&kfull[(it - 1) & 1], ((it - 1) >> 1) & 1, args.err);  // no MMA left in flight
+      if (unit > 0) wait_bar(pfull, (unit - 1) & 1, args.err);  // no MMA left in flight
     }
   } else {
-    // ---------------- accumulators + epilogue (warps 2..13) ----------------
+    // ---------------- worker warps (fold + interleaved epilogue) ----------------
     const int ew = warp - 2;              // 0 .. NEPI-1
     const int slice = warp & 3;           // TMEM lanes [32*slice, 32*slice + 32)
     const int grp = ew >> 2;              // column group: columns [80*grp, 80*grp + 80)
@@ -310,80 +334,116 @@ __global__ void __launch_bounds__(NTHREADS, 1) allpairs_tc_kernel(const __grid_c
     const int etid = ew * 32 + lane;      // 0 .. NEPI_THREADS-1
     const float inv_n = 1.0f / (float)args.A;
     const uint32_t lane_off = (uint32_t)(slice * 32) << 16;
-    uint32_t it = 0;
-    bool ok = true;
-    for (int64_t t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+    bool pend = false;   // a tile waits in R for its epilogue
+    int pass = 0;        // its next pass
+    int64_t pi0 = 0, pj0 = 0;
+
+    // One epilogue pass of the pending tile: the first pass of a chunk stages
+    // the chunk from R (one 16-column TMEM load per warp), then every thread
+    // takes at most one of the chunk's frame pairs.
+    auto do_pass = [&]() {
+      const int ch = pass / PASSES_PER_CHUNK, sub = pass % PASSES_PER_CHUNK;
+      if (sub == 0) {
+        if (CROSS && ch == 0 && etid < FR_N) colv[etid] = cross_col(args.reqs, args.colreq, pj0 + etid, args.n_b);
+        float v[16];
+        tc_ld16(tmem_base + R_COL + (uint32_t)(ch * EPI_COLS + grp * 16) + lane_off, v);
+        tc_wait_ld();
+        float* dst = sD + row * EPI_LD + grp * 16;
+#pragma unroll
+        for (int q = 0; q < 16; ++q) dst[q] = v[q];
+        named_bar(1, NEPI_THREADS);
+      }
+      const int p = sub * NEPI_THREADS + etid;
+      if (p < CHUNK_PAIRS) {
+        if (CROSS) {
+          // consecutive threads take consecutive row frames of one column frame:
+          // contiguous in the request's output row
+          const int lj = p / FR_M, li = p - lj * FR_M;
+          const int64_t i = pi0 + li;
+          const CrossCol cv = colv[ch * 16 + lj];
+          if (cv.row != nullptr && i >= cv.db0 && i < cv.db1 && i < args.F) {
+            float m[9];
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+#pragma unroll
+              for (int d = 0; d < 3; ++d) m[3 * c + d] = sD[(3 * li + c) * EPI_LD + 3 * lj + d];
+            const int64_t j = pj0 + ch * 16 + lj;
+            cross_pair(i, j, m, (float)args.G[i], (float)args.Gb[j], inv_n, cv.row + (i - cv.db0), args.rl,
+                       args.rc, args.rcap, args.err);
+          }
+        } else {
+          const int li = p >> 4, lj = p & 15;
+          const int64_t i = pi0 + li, j = pj0 + ch * 16 + lj;
+          if (i < args.F && j < args.F && i <= j) {
+            float m[9];
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+#pragma unroll
+              for (int d = 0; d < 3; ++d) m[3 * c + d] = sD[(3 * li + c) * EPI_LD + 3 * lj + d];
+            pair_epilogue(i, j, m, args.G, inv_n, args.F, args.out, args.rl, args.rc, args.rcap, args.err);
+          }
+        }
+      }
+      if (sub == PASSES_PER_CHUNK - 1) {
+        tc_fence_before();
+        named_bar(1, NEPI_THREADS);  // chunk (and, after the last, R) no longer read
+        tc_fence_after();
+      }
+      if (++pass == PASSES) pend = false;
+    };
+
+    uint32_t unit = 0;
+    bool failed = false;
+    for (int64_t t = blockIdx.x; t < n_tiles && !failed; t += gridDim.x) {
       float acc[GCOLS];
 #pragma unroll
       for (int q = 0; q < GCOLS; ++q) acc[q] = 0.f;
-      for (int kb = 0; kb < nkb; ++kb, ++it) {
-        const int b = it & 1;
-        if (ok && !wait_bar(&kfull[b], (it >> 1) & 1, args.err)) {
-          ok = false;
-          *fail_flag = 1;
+      for (int u = 0; u < nunit; ++u, ++unit) {
+        const bool ok = __all_sync(FULL_MASK, wait_bar(pfull, unit & 1, args.err) && !*fail_flag);
+        if (named_bar_or(2, NEPI_THREADS, !ok)) {  // one answer for all worker warps
+          failed = true;
+          break;
         }
-        if (ok) {
-          tc_fence_after();
-          const uint32_t taddr = tmem_base + (uint32_t)(b * ACC_STRIDE + grp * GCOLS) + lane_off;
+        tc_fence_after();
+        const uint32_t taddr = tmem_base + P_COL + (uint32_t)(grp * GCOLS) + lane_off;
 #pragma unroll
-          for (int c0 = 0; c0 < GCOLS; c0 += 16) {
-            float v[16];
-            tc_ld16(taddr + c0, v);
-            tc_wait_ld();
+        for (int c0 = 0; c0 < GCOLS; c0 += 16) {
+          float v[16];
+          tc_ld16(taddr + c0, v);
+          tc_wait_ld();
 #pragma unroll
-            for (int q = 0; q < 16; ++q) acc[c0 + q] += v[q];
-          }
-          tc_fence_before();
+          for (int q = 0; q < 16; ++q) acc[c0 + q] += v[q];
         }
+        tc_fence_before();
         __syncwarp();
-        if (ok && lane == 0) mbar_arrive(&kempty[b]);
+        if (lane == 0) mbar_arrive(pempty);
+        if (pend) do_pass();
       }
-      // the whole tile is in registers: stage it 48 columns (16 frames) at a time
-      named_bar(1, NEPI_THREADS);
-      const bool proceed = *fail_flag == 0;
-      const int2 tl = args.tiles[t];
-      const int64_t i0 = (int64_t)tl.x * FR_M, j0 = (int64_t)tl.y * FR_N;
-      if (CROSS && etid < FR_N) colv[etid] = cross_col(args.reqs, args.colreq, j0 + etid, args.n_b);
-      named_bar(1, NEPI_THREADS);
-      if (!proceed) break;
-      for (int ch = 0; ch < TILE_N / EPI_COLS; ++ch) {
-        stage_chunk(grp * (TILE_N / EPI_COLS) + ch, sD + row * EPI_LD, acc);
-        named_bar(1, NEPI_THREADS);
-        if (CROSS) {
-          // consecutive threads take consecutive database frames of one query
-          // column: contiguous in the request's output row
-          for (int p = etid; p < FR_M * 16; p += NEPI_THREADS) {
-            const int lj = p / FR_M, li = p - lj * FR_M;
-            const int64_t i = i0 + li;
-            const CrossCol cv = colv[ch * 16 + lj];
-            if (cv.row != nullptr && i >= cv.db0 && i < cv.db1 && i < args.F) {
-              float m[9];
+      if (failed) break;
+      while (pend) do_pass();  // R must be free before this tile goes in
+      {
+        const uint32_t taddr = tmem_base + R_COL + (uint32_t)(grp * GCOLS) + lane_off;
 #pragma unroll
-              for (int c = 0; c < 3; ++c)
+        for (int c0 = 0; c0 < GCOLS; c0 += 16) {
+          float v[16];
 #pragma unroll
-                for (int d = 0; d < 3; ++d) m[3 * c + d] = sD[(3 * li + c) * EPI_LD + 3 * lj + d];
-              const int64_t j = j0 + ch * 16 + lj;
-              cross_pair(i, j, m, (float)args.G[i], (float)args.Gb[j], inv_n, cv.row + (i - cv.db0), args.rl,
-                         args.rc, args.rcap, args.err);
-            }
-          }
-        } else {
-          for (int p = etid; p < FR_M * 16; p += NEPI_THREADS) {
-            const int li = p >> 4, lj = p & 15;
-            const int64_t i = i0 + li, j = j0 + ch * 16 + lj;
-            if (i < args.F && j < args.F && i <= j) {
-              float m[9];
-#pragma unroll
-              for (int c = 0; c < 3; ++c)
-#pragma unroll
-                for (int d = 0; d < 3; ++d) m[3 * c + d] = sD[(3 * li + c) * EPI_LD + 3 * lj + d];
-              pair_epilogue(i, j, m, args.G, inv_n, args.F, args.out, args.rl, args.rc, args.rcap, args.err);
-            }
-          }
+          for (int q = 0; q < 16; ++q) v[q] = acc[c0 + q];
+          tc_st16(taddr + c0, v);
         }
-        named_bar(1, NEPI_THREADS);
+        tc_wait_st();
       }
+      tc_fence_before();
+      named_bar(1, NEPI_THREADS);  // R complete for every worker warp
+      tc_fence_after();
+      const int2 tl = args.tiles[t];
+      pi0 = (int64_t)tl.x * FR_M;
+      pj0 = (int64_t)tl.y * FR_N;
+      pend = true;
+      pass = 0;
     }
+    if (failed) *fail_flag = 1;
+    else
+      while (pend) do_pass();
   }
 
   tc_fence_before();
