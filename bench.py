@@ -40,6 +40,29 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
+L2_BYTES = 129 << 20        # GB300 L2
+L2_FLUSH_BYTES = 256 << 20  # written between timed steps when the inputs fit in L2
+
+class L2Flush:
+    """Between timed steps: writes a 256 MB buffer (evicting everything the
+    previous step left in L2), then reads a second one so that the lines left
+    behind are clean and the next step's misses cause no write-backs of the
+    flush's own dirty data."""
+
+    def __init__(self, dev):
+        import torch
+
+        self.w = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+        self.r = torch.ones(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+        self.sink = torch.empty((), dtype=torch.float32, device=dev)
+
+    def __call__(self, i):
+        import torch
+
+        self.w.fill_(i & 0xFF)
+        torch.sum(self.r, dim=0, out=self.sink)
+
+
 WORKLOADS = {
     # name: (n_frames, n_atoms, layout, sigma_lo, sigma_hi, exact_fraction)
     "single_reference_200000x10000": (200_000, 10_000, 1, 0.005, 0.5, 0.01),
@@ -235,13 +258,33 @@ def run_gpu(args) -> dict:
     def step():
         _lib.check(lib.gbrmsd_rmsd_to_reference(x.data_ptr(), F, A, Ap, 3 * Ap, layout, _lib.MODE_CENTER,
                                                 dref.ws.data_ptr(), None, 0.0, -1, out.data_ptr(), None, None,
-                                                ws.data_ptr(), ws.numel(), stream))
+                                                ws.data_ptr(), ws.numel(), D.stream_handle()))
 
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
     _lib.check(lib.gbrmsd_workspace_status(ws.data_ptr(), stream))
-    lib.gbrmsd_profile_enable(args.steps)
+    # A working set that fits in L2 (120 MB at 10,000 x 1,000) is timed with
+    # a 256 MB write between steps, each step between its own events, and the
+    # step's launches replayed from a CUDA graph (the kernels take tens of
+    # microseconds, so launch overhead would otherwise show).
+    small = 12.0 * Ap * F < 4 * L2_BYTES
+    flush = L2Flush(dev) if small else None
+    graph = None
+    if small:
+        side = torch.cuda.Stream(device=dev)
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            step()
+        torch.cuda.current_stream().wait_stream(side)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            step()
+        for _ in range(args.warmup):
+            graph.replay()
+        torch.cuda.synchronize()
+    lib.gbrmsd_profile_enable(0 if small else args.steps)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     if world > 1:
@@ -249,13 +292,28 @@ def run_gpu(args) -> dict:
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
         e0.record()
-        for _ in range(args.steps):
-            step()
+        for i in range(args.steps):
+            if small:
+                flush(i)
+                ev[i][0].record()
+                graph.replay()
+                ev[i][1].record()
+            else:
+                step()
         e1.record()
         torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
-    ms_total = e0.elapsed_time(e1)
+    if small:
+        ms_total = float(sum(a.elapsed_time(b) for a, b in ev))
+        # the streaming kernel alone, outside the graph, flushed the same way
+        lib.gbrmsd_profile_enable(args.steps)
+        for i in range(args.steps):
+            flush(i + 7)
+            step()
+        torch.cuda.synchronize()
+    else:
+        ms_total = e0.elapsed_time(e1)
     kms = np.zeros(args.steps, dtype=np.float32)
     nk = lib.gbrmsd_profile_read(kms.ctypes.data, args.steps)
     lib.gbrmsd_profile_enable(0)
@@ -303,7 +361,9 @@ def run_gpu(args) -> dict:
         "config": {"workload": args.workload, "n_frames": F, "n_atoms": A,
                    "layout": "axis-major" if layout == 1 else "atom-major", "precentered": False,
                    "sigma_nm": [s_lo, s_hi], "exact_copy_fraction": exact,
-                   "l2": "inputs (%.1f GB) larger than L2; no flush" % (12.0 * Ap * F / 1e9),
+                   "l2": ("inputs (%.3f GB) fit in L2: 256 MB write + 256 MB read between steps, each step timed alone, "
+                          "launches replayed from a CUDA graph" % (12.0 * Ap * F / 1e9)) if small else
+                         "inputs (%.1f GB) larger than L2; no flush" % (12.0 * Ap * F / 1e9),
                    "parallelism": f"frame shards x{world}"},
         "roofline": roof,
         "cpu_baseline": cpu_base,
@@ -378,10 +438,12 @@ def run_e2e(args, F, A, s_lo, s_hi, exact, dev) -> dict:
         md.rmsd(target, reference, 0)
         times.append(time.perf_counter() - t0)
     t = float(np.mean(times))
+    # inbound: every frame and the reference frame; outbound: one RMSD per
+    # frame and the in-place centring of every frame written back
     return {"value": round(Fe / t, 1), "unit": "frames/s", "h2d_bytes_per_step": int(Fe * A * 12 + A * 12),
-            "d2h_bytes_per_step": int(Fe * 4 + Fe * 12), "ms_per_step": round(t * 1e3, 2),
+            "d2h_bytes_per_step": int(Fe * 4 + Fe * A * 12), "ms_per_step": round(t * 1e3, 2),
             "frames": Fe, "api": "mdtraj_gb300.rmsd(target, reference, 0) on host float32 arrays",
-            "steps": args.e2e_steps}
+            "steps": args.e2e_steps, "step_ms": [round(x * 1e3, 2) for x in times]}
 
 
 # ---------------------------------------------------------------------------
@@ -1228,7 +1290,7 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
     ap.add_argument("--frames", type=int, default=None, help="override n_frames (smaller runs)")
     ap.add_argument("--e2e-frames", type=int, default=None)
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU baseline work")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")

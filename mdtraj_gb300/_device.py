@@ -201,14 +201,17 @@ def _side_streams(device) -> tuple[torch.cuda.Stream, torch.cuda.Stream]:
 
 def rmsd_host_frames(x: np.ndarray, ref: "DeviceReference", mode: int, *, g_target: np.ndarray | None = None,
                      g_ref: float = 0.0, self_index: int = -1, write_centred: bool = False,
-                     chunk_bytes: int = 256 << 20, ring: int = 3) -> np.ndarray:
+                     chunk_bytes: int = 256 << 20, ring: int = 2) -> np.ndarray:
     """RMSD of every frame of a HOST atom-major array (F, A, 3) float32 to a
     prepared reference, streamed through the GPU in chunks.
 
-    Chunk k's host->device copy (stream 1) overlaps the kernels and, with
-    `write_centred`, the in-place centring write-back of chunk k-1 (stream 2),
-    so the two directions of the host link run concurrently.  A ring of
-    `ring` device chunk buffers bounds device memory.  Returns float32 (F,).
+    Chunk k+1's host->device copy (stream 1) runs together with chunk k's
+    in-place centring write-back (stream 2), so both directions of the host
+    link are busy at once; the RMSD kernels of chunk k run between the two
+    phases, alone on the GPU (the persistent streaming kernel needs a whole
+    SM's registers, which the copy kernels would otherwise hold until they
+    end).  A ring of `ring` (>= 2) device chunk buffers bounds device memory.
+    Returns float32 (F,).
     """
     device = require_device()
     F, A = x.shape[0], x.shape[1]
@@ -229,17 +232,20 @@ def rmsd_host_frames(x: np.ndarray, ref: "DeviceReference", mode: int, *, g_targ
     ws = empty_bytes(lib.gbrmsd_rmsd_workspace_bytes(C, A), device)
     host_ok = pageable_access()
     in_done = [torch.cuda.Event() for _ in range(n_chunks)]
-    work_done = [torch.cuda.Event() for _ in range(n_chunks)]
+    rmsd_done = [torch.cuda.Event() for _ in range(n_chunks)]
     s_in.wait_stream(cur)
     s_work.wait_stream(cur)
+    assert len(bufs) >= 2 or n_chunks == 1
     for k in range(n_chunks):
         f0 = k * C
         n = min(C, F - f0)
         buf = bufs[k % len(bufs)]
         src = x.ctypes.data + f0 * 12 * A
         with torch.cuda.stream(s_in):
-            if k >= len(bufs):
-                s_in.wait_event(work_done[k - len(bufs)])
+            if k >= 1:
+                # after chunk k-1's RMSD kernels (which follow chunk k-2's
+                # write-back on stream 2, so buffer k % ring is free again)
+                s_in.wait_event(rmsd_done[k - 1])
             if host_ok:
                 check(lib.gbrmsd_copy_rows_kernel(buf.data_ptr(), 3 * Ap, src, 3 * A, 3 * A, 3 * Ap, n,
                                                   s_in.cuda_stream))
@@ -254,12 +260,12 @@ def rmsd_host_frames(x: np.ndarray, ref: "DeviceReference", mode: int, *, g_targ
                 ptr(g_dev[f0:f0 + n]) if g_dev is not None else None, float(g_ref), si,
                 out[f0:f0 + n].data_ptr(), cent[f0:f0 + n].data_ptr() if cent is not None else None, None,
                 ws.data_ptr(), ws.numel(), s_work.cuda_stream))
+            rmsd_done[k].record(s_work)
             if write_centred:
                 dst = x.ctypes.data + f0 * 12 * A
                 if host_ok:
                     check(lib.gbrmsd_write_centred(dst, buf.data_ptr(), 3 * Ap, cent[f0:f0 + n].data_ptr(), n, A,
                                                    s_work.cuda_stream))
-            work_done[k].record(s_work)
     result = np.empty(F, dtype=np.float32)
     copy_rows(result.ctypes.data, 4 * F, out.data_ptr(), 4 * F, 4 * F, 1, 2, s_work.cuda_stream)
     s_work.synchronize()

@@ -330,6 +330,14 @@ __global__ void __launch_bounds__(WARPS * 32, 1) stream_kernel(const StreamArgs 
 // QCP finish: one thread per frame
 // ---------------------------------------------------------------------------
 
+// Threads per finish block: the QCP solve is FP64 (a narrow pipe on GB300),
+// so batches of fewer than ~2 frames per thread slot of the whole GPU are
+// spread over every SM with 64-thread blocks instead of packing 256 frames
+// into each of a few blocks.
+int finish_threads(int64_t n_frames) { return n_frames >= 256LL * 2 * sm_count() ? 256 : 64; }
+
+void launch_finish(const FinishArgs& fa, int64_t n_frames, cudaStream_t st);
+
 __global__ void __launch_bounds__(256) finish_kernel(const FinishArgs a) {
   const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= a.n_frames) return;
@@ -349,6 +357,11 @@ __global__ void __launch_bounds__(256) finish_kernel(const FinishArgs a) {
   c.out_rot = a.out_rot;
   c.out_mu = a.out_mu;
   finish_frame(c, a.out_rmsd, a.out_centroid, a.out_trace, a.refine, a.refine_count, a.err);
+}
+
+void launch_finish(const FinishArgs& fa, int64_t n_frames, cudaStream_t st) {
+  const int t = finish_threads(n_frames);
+  finish_kernel<<<(unsigned)((n_frames + t - 1) / t), t, 0, st>>>(fa);
 }
 
 // ---------------------------------------------------------------------------
@@ -815,8 +828,7 @@ int gbrmsd_rmsd_to_reference(const float* x, int64_t n_frames, int32_t n_atoms, 
   fa.mode = mode;
   fa.out_rot = nullptr;
   fa.out_mu = nullptr;
-  const int fb = (int)((n_frames + 255) / 256);
-  finish_kernel<<<fb, 256, 0, st>>>(fa);
+  launch_finish(fa, n_frames, st);
   GB_CUDA_TRY(cudaGetLastError(), "launch finish_kernel");
 
   if (mode != MODE_NOSUPERPOSE) {
@@ -894,7 +906,7 @@ int gbrmsd_rotations(const float* x, int64_t n_frames, int32_t n_atoms, int32_t 
   fa.mode = mode;
   fa.out_rot = out_rot;
   fa.out_mu = mode == MODE_CENTER ? out_centroid : nullptr;
-  finish_kernel<<<(int)((n_frames + 255) / 256), 256, 0, st>>>(fa);
+  launch_finish(fa, n_frames, st);
   GB_CUDA_TRY(cudaGetLastError(), "launch finish_kernel (rotations)");
   if (out_rmsd) {  // exact rmsd for near-identical frames, as gbrmsd_rmsd_to_reference
     RefineArgs ra;
@@ -997,7 +1009,7 @@ int gbrmsd_center_inplace(float* x, int64_t n_frames, int32_t n_atoms, int32_t n
   fa.err = &hdr->err;
   fa.mode = MODE_TRACE;
   fa.self_index = -1;
-  finish_kernel<<<(int)((n_frames + 255) / 256), 256, 0, st>>>(fa);
+  launch_finish(fa, n_frames, st);
   GB_CUDA_TRY(cudaGetLastError(), "launch finish_kernel(trace)");
   const int grid = sm_count() * 4;
   if (layout == ATOM_MAJOR)
