@@ -31,41 +31,71 @@ struct AllPairsDims {
 
 constexpr int DEV_ERR_REFINE_OVERFLOW = 4;
 
+// Explicitly rounded FP32 operations for the pair epilogue.  The epilogue is
+// inlined at several points of the tile kernels (inside the fold loop, after
+// it, at the end of a CTA's tiles), and with implicit contraction the
+// compiler is free to fuse a product into an FMA at one point and not at
+// another; a pair would then round differently depending on where in its
+// CTA's tile sequence it was finished, and a query served in a mixed batch
+// could differ in the last bit from the same query served alone.  The _rn
+// intrinsics are never contracted, so every copy computes the same bits.
+__device__ __forceinline__ float rn_mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float rn_add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float rn_sub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float rn_fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+// a b - c d
+__device__ __forceinline__ float rn_det2(float a, float b, float c, float d) { return rn_fma(a, b, rn_mul(-c, d)); }
+// a0 b0 + a1 b1 + a2 b2 (+ a3 b3)
+__device__ __forceinline__ float rn_dot3(float a0, float b0, float a1, float b1, float a2, float b2) {
+  return rn_fma(a2, b2, rn_fma(a1, b1, rn_mul(a0, b0)));
+}
+__device__ __forceinline__ float rn_dot4(float a0, float b0, float a1, float b1, float a2, float b2, float a3,
+                                         float b3) {
+  return rn_fma(a3, b3, rn_fma(a2, b2, rn_fma(a1, b1, rn_mul(a0, b0))));
+}
+
 // FP32 QCP on the quartic normalised by lam0 = (Ga + Gb) / 2 (root near 1).
-// Returns msd = 2 lam0 (1 - x) / n; *x_out = normalised lambda_max.
+// Returns msd = 2 lam0 (1 - x) / n, x = normalised lambda_max.
 __device__ __forceinline__ float qcp_msd_f32(const float (&m)[9], float ga, float gb, float inv_n) {
-  const float lam0 = 0.5f * (ga + gb);
+  const float lam0 = rn_mul(0.5f, rn_add(ga, gb));
   if (!(lam0 > 0.f)) return 0.f;
-  const float inv = 1.0f / lam0;
+  const float inv = __fdiv_rn(1.0f, lam0);
   float mm[9];
 #pragma unroll
-  for (int t = 0; t < 9; ++t) mm[t] = m[t] * inv;
-  const float k00 = mm[0] + mm[4] + mm[8], k01 = mm[5] - mm[7], k02 = mm[6] - mm[2], k03 = mm[1] - mm[3];
-  const float k11 = mm[0] - mm[4] - mm[8], k12 = mm[1] + mm[3], k13 = mm[6] + mm[2];
-  const float k22 = -mm[0] + mm[4] - mm[8], k23 = mm[5] + mm[7], k33 = -mm[0] - mm[4] + mm[8];
+  for (int t = 0; t < 9; ++t) mm[t] = rn_mul(m[t], inv);
+  const float k00 = rn_add(rn_add(mm[0], mm[4]), mm[8]), k01 = rn_sub(mm[5], mm[7]);
+  const float k02 = rn_sub(mm[6], mm[2]), k03 = rn_sub(mm[1], mm[3]);
+  const float k11 = rn_sub(rn_sub(mm[0], mm[4]), mm[8]), k12 = rn_add(mm[1], mm[3]), k13 = rn_add(mm[6], mm[2]);
+  const float k22 = rn_sub(rn_sub(mm[4], mm[0]), mm[8]), k23 = rn_add(mm[5], mm[7]);
+  const float k33 = rn_sub(rn_sub(mm[8], mm[0]), mm[4]);
   float c2 = 0.f;
 #pragma unroll
-  for (int t = 0; t < 9; ++t) c2 = fmaf(mm[t], mm[t], c2);
-  c2 *= -2.f;
-  const float detm = mm[0] * (mm[4] * mm[8] - mm[5] * mm[7]) - mm[1] * (mm[3] * mm[8] - mm[5] * mm[6]) +
-                     mm[2] * (mm[3] * mm[7] - mm[4] * mm[6]);
-  const float c1 = -8.f * detm;
-  const float s01 = k00 * k11 - k01 * k01, s02 = k00 * k12 - k02 * k01, s03 = k00 * k13 - k03 * k01;
-  const float s12 = k01 * k12 - k02 * k11, s13 = k01 * k13 - k03 * k11, s23 = k02 * k13 - k03 * k12;
-  const float q01 = k02 * k13 - k12 * k03, q02 = k02 * k23 - k22 * k03, q03 = k02 * k33 - k23 * k03;
-  const float q12 = k12 * k23 - k22 * k13, q13 = k12 * k33 - k23 * k13, q23 = k22 * k33 - k23 * k23;
-  const float c0 = s01 * q23 - s02 * q13 + s03 * q12 + s12 * q03 - s13 * q02 + s23 * q01;
+  for (int t = 0; t < 9; ++t) c2 = rn_fma(mm[t], mm[t], c2);
+  c2 = rn_mul(c2, -2.f);
+  const float detm = rn_dot3(mm[0], rn_det2(mm[4], mm[8], mm[5], mm[7]), -mm[1], rn_det2(mm[3], mm[8], mm[5], mm[6]),
+                             mm[2], rn_det2(mm[3], mm[7], mm[4], mm[6]));
+  const float c1 = rn_mul(-8.f, detm);
+  const float s01 = rn_det2(k00, k11, k01, k01), s02 = rn_det2(k00, k12, k02, k01), s03 = rn_det2(k00, k13, k03, k01);
+  const float s12 = rn_det2(k01, k12, k02, k11), s13 = rn_det2(k01, k13, k03, k11), s23 = rn_det2(k02, k13, k03, k12);
+  const float q01 = rn_det2(k02, k13, k12, k03), q02 = rn_det2(k02, k23, k22, k03), q03 = rn_det2(k02, k33, k23, k03);
+  const float q12 = rn_det2(k12, k23, k22, k13), q13 = rn_det2(k12, k33, k23, k13), q23 = rn_det2(k22, k33, k23, k23);
+  float c0 = rn_mul(s01, q23);
+  c0 = rn_fma(-s02, q13, c0);
+  c0 = rn_fma(s03, q12, c0);
+  c0 = rn_fma(s12, q03, c0);
+  c0 = rn_fma(-s13, q02, c0);
+  c0 = rn_fma(s23, q01, c0);
   float x = 1.0f;
 #pragma unroll 1
   for (int it = 0; it < 30; ++it) {
-    const float x2 = x * x;
-    const float b = (x2 + c2) * x;
-    const float a = b + c1;
-    const float pv = a * x + c0;
-    const float dp = 2.0f * x2 * x + b + a;
+    const float x2 = rn_mul(x, x);
+    const float b = rn_mul(rn_add(x2, c2), x);
+    const float a = rn_add(b, c1);
+    const float pv = rn_fma(a, x, c0);
+    const float dp = rn_add(rn_fma(rn_mul(2.0f, x2), x, b), a);
     if (!(dp != 0.0f)) break;
     const float step = __fdividef(pv, dp);
-    x -= step;
+    x = rn_sub(x, step);
     if (!(fabsf(step) > 2e-7f)) break;
   }
   // The quartic's largest root is ill-conditioned when the top eigenvalues of
@@ -76,51 +106,58 @@ __device__ __forceinline__ float qcp_msd_f32(const float (&m)[9], float ga, floa
   // quadratic in v's): x += v^T (K - x I) v / v^T v.  The adjugate comes from
   // the 2x2 complementary minors of rows {0,1} and {2,3} (Laplace expansion).
   {
-    const float b00 = k00 - x, b11 = k11 - x, b22 = k22 - x, b33 = k33 - x;
+    const float b00 = rn_sub(k00, x), b11 = rn_sub(k11, x), b22 = rn_sub(k22, x), b33 = rn_sub(k33, x);
     const float b01 = k01, b02 = k02, b03 = k03, b12 = k12, b13 = k13, b23 = k23;
-    const float u0 = b00 * b11 - b01 * b01, u1 = b00 * b12 - b01 * b02, u2 = b00 * b13 - b01 * b03;
-    const float u3 = b01 * b12 - b11 * b02, u4 = b01 * b13 - b11 * b03, u5 = b02 * b13 - b12 * b03;
-    const float w5 = b22 * b33 - b23 * b23, w4 = b12 * b33 - b13 * b23, w3 = b12 * b23 - b13 * b22;
-    const float w2 = b02 * b33 - b03 * b23, w1 = b02 * b23 - b03 * b22, w0 = b02 * b13 - b03 * b12;
-    const float a00 = b11 * w5 - b12 * w4 + b13 * w3;
-    const float a11 = b00 * w5 - b02 * w2 + b03 * w1;
-    const float a22 = b03 * u4 - b13 * u2 + b33 * u0;
-    const float a33 = b02 * u3 - b12 * u1 + b22 * u0;
+    const float u0 = rn_det2(b00, b11, b01, b01), u1 = rn_det2(b00, b12, b01, b02), u2 = rn_det2(b00, b13, b01, b03);
+    const float u3 = rn_det2(b01, b12, b11, b02), u4 = rn_det2(b01, b13, b11, b03), u5 = rn_det2(b02, b13, b12, b03);
+    const float w5 = rn_det2(b22, b33, b23, b23), w4 = rn_det2(b12, b33, b13, b23), w3 = rn_det2(b12, b23, b13, b22);
+    const float w2 = rn_det2(b02, b33, b03, b23), w1 = rn_det2(b02, b23, b03, b22), w0 = rn_det2(b02, b13, b03, b12);
+    const float a00 = rn_dot3(b11, w5, -b12, w4, b13, w3);
+    const float a11 = rn_dot3(b00, w5, -b02, w2, b03, w1);
+    const float a22 = rn_dot3(b03, u4, -b13, u2, b33, u0);
+    const float a33 = rn_dot3(b02, u3, -b12, u1, b22, u0);
     float v0, v1, v2, v3, best = fabsf(a00);
     v0 = a00;
-    v1 = -b01 * w5 + b02 * w4 - b03 * w3;
-    v2 = b13 * u5 - b23 * u4 + b33 * u3;
-    v3 = -b12 * u5 + b22 * u4 - b23 * u3;
+    v1 = rn_dot3(-b01, w5, b02, w4, -b03, w3);
+    v2 = rn_dot3(b13, u5, -b23, u4, b33, u3);
+    v3 = rn_dot3(-b12, u5, b22, u4, -b23, u3);
     if (fabsf(a11) > best) {
       best = fabsf(a11);
-      v0 = -b01 * w5 + b12 * w2 - b13 * w1;
+      v0 = rn_dot3(-b01, w5, b12, w2, -b13, w1);
       v1 = a11;
-      v2 = -b03 * u5 + b23 * u2 - b33 * u1;
-      v3 = b02 * u5 - b22 * u2 + b23 * u1;
+      v2 = rn_dot3(-b03, u5, b23, u2, -b33, u1);
+      v3 = rn_dot3(b02, u5, -b22, u2, b23, u1);
     }
     if (fabsf(a22) > best) {
       best = fabsf(a22);
-      v0 = b01 * w4 - b11 * w2 + b13 * w0;
-      v1 = -b00 * w4 + b01 * w2 - b03 * w0;
+      v0 = rn_dot3(b01, w4, -b11, w2, b13, w0);
+      v1 = rn_dot3(-b00, w4, b01, w2, -b03, w0);
       v2 = a22;
-      v3 = -b02 * u4 + b12 * u2 - b23 * u0;
+      v3 = rn_dot3(-b02, u4, b12, u2, -b23, u0);
     }
     if (fabsf(a33) > best) {
-      v0 = -b01 * w3 + b11 * w1 - b12 * w0;
-      v1 = b00 * w3 - b01 * w1 + b02 * w0;
-      v2 = -b03 * u3 + b13 * u1 - b23 * u0;
+      v0 = rn_dot3(-b01, w3, b11, w1, -b12, w0);
+      v1 = rn_dot3(b00, w3, -b01, w1, b02, w0);
+      v2 = rn_dot3(-b03, u3, b13, u1, -b23, u0);
       v3 = a33;
     }
-    const float bv0 = b00 * v0 + b01 * v1 + b02 * v2 + b03 * v3;
-    const float bv1 = b01 * v0 + b11 * v1 + b12 * v2 + b13 * v3;
-    const float bv2 = b02 * v0 + b12 * v1 + b22 * v2 + b23 * v3;
-    const float bv3 = b03 * v0 + b13 * v1 + b23 * v2 + b33 * v3;
-    const float vv = v0 * v0 + v1 * v1 + v2 * v2 + v3 * v3;
-    const float dx = (v0 * bv0 + v1 * bv1 + v2 * bv2 + v3 * bv3) / vv;
-    if (vv > 1e-30f && fabsf(dx) < 1e-3f) x += dx;
+    const float bv0 = rn_dot4(b00, v0, b01, v1, b02, v2, b03, v3);
+    const float bv1 = rn_dot4(b01, v0, b11, v1, b12, v2, b13, v3);
+    const float bv2 = rn_dot4(b02, v0, b12, v1, b22, v2, b23, v3);
+    const float bv3 = rn_dot4(b03, v0, b13, v1, b23, v2, b33, v3);
+    const float vv = rn_dot4(v0, v0, v1, v1, v2, v2, v3, v3);
+    const float dx = __fdiv_rn(rn_dot4(v0, bv0, v1, bv1, v2, bv2, v3, bv3), vv);
+    if (vv > 1e-30f && fabsf(dx) < 1e-3f) x = rn_add(x, dx);
   }
-  const float msd = 2.0f * lam0 * (1.0f - x) * inv_n;
+  const float msd = rn_mul(rn_mul(rn_mul(2.0f, lam0), rn_sub(1.0f, x)), inv_n);
   return msd > 0.f ? msd : 0.f;
+}
+
+// Refinement threshold of a pair: r < 0.25 * scale * sqrt(1/n), scale =
+// (Ga + Gb) / 2n (explicitly rounded for the same reason as the QCP above).
+__device__ __forceinline__ bool pair_needs_refine(float r, float ga, float gb, float inv_n) {
+  const float scale = rn_mul(rn_mul(0.5f, rn_add(ga, gb)), inv_n);
+  return r < rn_mul(rn_mul(0.25f, scale), sqrtf(inv_n));
 }
 
 // Writes the pair's rmsd to both triangles (i < j) or 0 on the diagonal and
@@ -140,8 +177,7 @@ __device__ __forceinline__ void pair_epilogue(int64_t i, int64_t j, const float 
   const float r = sqrtf(msd);
   out[i * F + j] = r;
   out[j * F + i] = r;
-  const float scale = 0.5f * (ga + gb) * inv_n;
-  if (r < 0.25f * scale * sqrtf(inv_n)) {
+  if (pair_needs_refine(r, ga, gb, inv_n)) {
     const int slot = atomicAdd(rc, 1);
     if (slot < rcap)
       rl[slot] = PairRefine{(int32_t)i, (int32_t)j};
@@ -183,8 +219,7 @@ __device__ __forceinline__ void cross_pair(int64_t i, int64_t j, const float (&m
   const float msd = qcp_msd_f32(m, ga, gb, inv_n);
   const float r = sqrtf(msd);
   *dst = r;
-  const float scale = 0.5f * (ga + gb) * inv_n;
-  if (r < 0.25f * scale * sqrtf(inv_n)) {
+  if (pair_needs_refine(r, ga, gb, inv_n)) {
     const int slot = atomicAdd(rc, 1);
     if (slot < rcap)
       rl[slot] = PairRefine{(int32_t)i, (int32_t)j};

@@ -101,6 +101,12 @@ __host__ __device__ __forceinline__ double qcp_lambda_max(const double* m, doubl
 // root is near 1 and nothing overflows), then FP64 Newton steps on the
 // original FP64 coefficients polish it to double precision (quadratic
 // convergence from a 1e-7-accurate start: usually one or two steps).
+// No FP64 division: the normalisation only has to be close to 1 / lam0 (the
+// polish works on the unnormalised quartic), and a polish step of relative
+// size ~1e-7 needs its quotient to FP32 precision only (an error of 1e-7 in
+// a step of 1e-7 * lam moves lam by 1e-14 relative), so both use an FP32
+// reciprocal; FP64 division remains only where FP32 would over- or
+// underflow.
 __host__ __device__ __forceinline__ double qcp_lambda_max_mixed(const double* m, double ga, double gb,
                                                                 int* iters, int max_iter = 60) {
   const Key4 k = key_matrix(m);
@@ -115,7 +121,9 @@ __host__ __device__ __forceinline__ double qcp_lambda_max_mixed(const double* m,
     if (iters) *iters = 0;
     return 0.0;
   }
-  const double inv = 1.0 / lam0;
+  const float lam0f = (float)lam0;
+  double inv = (double)(1.0f / lam0f);
+  if (!(lam0f > 1e-30f) || !(lam0f < 1e30f)) inv = 1.0 / lam0;
   const double inv2 = inv * inv;
   const float a2 = (float)(c2 * inv2);
   const float a1 = (float)(c1 * inv2 * inv);
@@ -146,7 +154,8 @@ __host__ __device__ __forceinline__ double qcp_lambda_max_mixed(const double* m,
     const double pv = a * lam + c0;
     const double dp = 2.0 * l2 * lam + b + a;
     if (!(dp != 0.0)) break;
-    const double step = pv / dp;
+    const float dpf = (float)fabs(dp);
+    const double step = (dpf > 1e-30f && dpf < 1e30f) ? pv * (double)(1.0f / (float)dp) : pv / dp;
     lam -= step;
     if (!(fabs(step) > 1e-15 * fabs(lam))) {
       ++jt;

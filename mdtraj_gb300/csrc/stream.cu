@@ -538,16 +538,34 @@ StreamCfg choose_cfg(int32_t Ap, bool use_ref) {
 
 int grid_warps(const StreamCfg& c) { return sm_count() * c.warps; }
 
+// Splits per frame: frames are cut into S units of Q/S quads so that every
+// warp gets work, but each unit also costs a fixed epilogue (shift, warp
+// reduction of 13 compensated sums, record).  S minimises the busiest warp's
+// time, ceil(F S / warps) * (Q/S * kCyclesPerQuad + kCyclesPerUnit): ~35
+// cycles per 48-byte quad is a warp's share of the HBM bandwidth with 16
+// warps per SM, ~3,400 cycles the per-unit epilogue (about 850 warp
+// instructions at a quarter of an SMSP's issue rate; measured with ncu at
+// 10,000 x 1,000 atoms, where S = 4 spent 1,000 instructions per 62-quad
+// unit and ran at 0.3 of the copy peak).
 int32_t choose_splits(int64_t F, int32_t Q, int gwarps) {
-  if (F <= 0) return 1;
-  const int64_t target = 16LL * gwarps;
-  if (F >= target) return 1;
-  int64_t s = (target + F - 1) / F;
+  constexpr double kCyclesPerQuad = 35.0, kCyclesPerUnit = 3400.0;
+  if (F <= 0 || gwarps <= 0) return 1;
   int64_t smax = Q / 32;
   if (smax < 1) smax = 1;
-  if (s > smax) s = smax;
-  if (s < 1) s = 1;
-  return (int32_t)s;
+  // beyond ~64 units per warp more splits only add epilogues
+  const int64_t scap = (64LL * gwarps + F - 1) / F;
+  if (smax > scap) smax = scap;
+  int32_t best_s = 1;
+  double best = 0.0;
+  for (int64_t s = 1; s <= smax; ++s) {
+    const double per_warp = (double)((F * s + gwarps - 1) / gwarps);
+    const double cost = per_warp * ((double)Q / (double)s * kCyclesPerQuad + kCyclesPerUnit);
+    if (s == 1 || cost < best * 0.999) {
+      best = cost;
+      best_s = (int32_t)s;
+    }
+  }
+  return best_s;
 }
 
 template <int LAYOUT, int MODE, int CQ, int NSTAGE, bool REF_SMEM, int WARPS>
@@ -841,7 +859,8 @@ int gbrmsd_rmsd_to_reference(const float* x, int64_t n_frames, int32_t n_atoms, 
     ra.list = fa.refine;
     ra.count = fa.refine_count;
     ra.out_rmsd = out_rmsd;
-    const int rgrid = sm_count() * 4;
+    // one warp per queued frame; the queue is usually short or empty
+    const int rgrid = sm_count() * 2;
     if (layout == ATOM_MAJOR)
       refine_kernel<ATOM_MAJOR><<<rgrid, 256, 0, st>>>(ra);
     else

@@ -249,12 +249,13 @@ __device__ __forceinline__ void finish_frame(const FrameCtx& c, float* out_rmsd,
   const int32_t Q = (A + 3) >> 2;
   const double* base = c.recs;
   const double dA = (double)A;
+  const double invA = 1.0 / dA;  // the frame's one FP64 division (a narrow pipe on GB300)
   const int64_t f = c.out_idx;
 
   if (c.mode == MODE_NOSUPERPOSE) {
     double g = 0.0;
     for (int j = 0; j < S; ++j) g += base[j * SUMS_STRIDE + 12];
-    double msd = g / dA;
+    double msd = g * invA;
     if (!(msd > 0.0)) msd = 0.0;
     out_rmsd[f] = (float)sqrt(msd);
     return;
@@ -263,7 +264,7 @@ __device__ __forceinline__ void finish_frame(const FrameCtx& c, float* out_rmsd,
     for (int k = 0; k < 3; ++k) {
       double s = 0.0;
       for (int j = 0; j < S; ++j) s += base[j * SUMS_STRIDE + 9 + k];
-      out_centroid[3 * f + k] = (float)(s / dA);
+      out_centroid[3 * f + k] = (float)(s * invA);
     }
     return;
   }
@@ -283,7 +284,7 @@ __device__ __forceinline__ void finish_frame(const FrameCtx& c, float* out_rmsd,
       const double nj = (double)(min(4 * q1, A) - 4 * q0);
       for (int k = 0; k < 3; ++k) sa[k] += r[9 + k] + nj * r[16 + k];
     }
-    for (int k = 0; k < 3; ++k) mu[k] = sa[k] / dA;
+    for (int k = 0; k < 3; ++k) mu[k] = sa[k] * invA;
     ga = 0.0;
     for (int j = 0; j < S; ++j) {
       const double* r = base + j * SUMS_STRIDE;
@@ -322,7 +323,7 @@ __device__ __forceinline__ void finish_frame(const FrameCtx& c, float* out_rmsd,
   }
   int iters = 0;
   const double lam = qcp_lambda_max_mixed(m, ga, gb, &iters);
-  double msd = (ga + gb - 2.0 * lam) / dA;
+  double msd = (ga + gb - 2.0 * lam) * invA;
   if (!(msd > 0.0) || self) msd = 0.0;
   out_rmsd[f] = sqrtf((float)msd);
   if (c.out_rot) {
@@ -337,7 +338,7 @@ __device__ __forceinline__ void finish_frame(const FrameCtx& c, float* out_rmsd,
   // One-pass sums resolve msd to about 1e-7 * scale / sqrt(A); below
   // (0.1 * scale / sqrt(A))^2 the direct residual is recomputed by the
   // refinement kernel.  scale = (G_a + G_b) / (2 A).
-  const double scale = (ga + gb) / (2.0 * dA);
+  const double scale = (ga + gb) * (0.5 * invA);
   if (msd * dA < 0.01 * scale * scale && A > 0) {
     double rot[9];
     qcp_rotation(m, lam, rot);
