@@ -236,36 +236,43 @@ def rmsd_host_frames(x: np.ndarray, ref: "DeviceReference", mode: int, *, g_targ
     s_in.wait_stream(cur)
     s_work.wait_stream(cur)
     assert len(bufs) >= 2 or n_chunks == 1
-    for k in range(n_chunks):
-        f0 = k * C
-        n = min(C, F - f0)
-        buf = bufs[k % len(bufs)]
-        src = x.ctypes.data + f0 * 12 * A
-        with torch.cuda.stream(s_in):
-            if k >= 1:
-                # after chunk k-1's RMSD kernels (which follow chunk k-2's
-                # write-back on stream 2, so buffer k % ring is free again)
-                s_in.wait_event(rmsd_done[k - 1])
-            if host_ok:
-                check(lib.gbrmsd_copy_rows_kernel(buf.data_ptr(), 3 * Ap, src, 3 * A, 3 * A, 3 * Ap, n,
-                                                  s_in.cuda_stream))
-            else:
-                copy_rows(buf.data_ptr(), 12 * Ap, src, 12 * A, 12 * A, n, 1, s_in.cuda_stream)
-            in_done[k].record(s_in)
-        with torch.cuda.stream(s_work):
-            s_work.wait_event(in_done[k])
-            si = self_index - f0 if 0 <= self_index - f0 < n else -1
-            check(lib.gbrmsd_rmsd_to_reference(
-                buf.data_ptr(), n, A, Ap, 3 * Ap, _lib.ATOM_MAJOR, mode, ref.ws.data_ptr(),
-                ptr(g_dev[f0:f0 + n]) if g_dev is not None else None, float(g_ref), si,
-                out[f0:f0 + n].data_ptr(), cent[f0:f0 + n].data_ptr() if cent is not None else None, None,
-                ws.data_ptr(), ws.numel(), s_work.cuda_stream))
-            rmsd_done[k].record(s_work)
-            if write_centred:
-                dst = x.ctypes.data + f0 * 12 * A
+    try:
+        for k in range(n_chunks):
+            f0 = k * C
+            n = min(C, F - f0)
+            buf = bufs[k % len(bufs)]
+            src = x.ctypes.data + f0 * 12 * A
+            with torch.cuda.stream(s_in):
+                if k >= 1:
+                    # after chunk k-1's RMSD kernels (which follow chunk k-2's
+                    # write-back on stream 2, so buffer k % ring is free again)
+                    s_in.wait_event(rmsd_done[k - 1])
                 if host_ok:
-                    check(lib.gbrmsd_write_centred(dst, buf.data_ptr(), 3 * Ap, cent[f0:f0 + n].data_ptr(), n, A,
-                                                   s_work.cuda_stream))
+                    check(lib.gbrmsd_copy_rows_kernel(buf.data_ptr(), 3 * Ap, src, 3 * A, 3 * A, 3 * Ap, n,
+                                                      s_in.cuda_stream))
+                else:
+                    copy_rows(buf.data_ptr(), 12 * Ap, src, 12 * A, 12 * A, n, 1, s_in.cuda_stream)
+                in_done[k].record(s_in)
+            with torch.cuda.stream(s_work):
+                s_work.wait_event(in_done[k])
+                si = self_index - f0 if 0 <= self_index - f0 < n else -1
+                check(lib.gbrmsd_rmsd_to_reference(
+                    buf.data_ptr(), n, A, Ap, 3 * Ap, _lib.ATOM_MAJOR, mode, ref.ws.data_ptr(),
+                    ptr(g_dev[f0:f0 + n]) if g_dev is not None else None, float(g_ref), si,
+                    out[f0:f0 + n].data_ptr(), cent[f0:f0 + n].data_ptr() if cent is not None else None, None,
+                    ws.data_ptr(), ws.numel(), s_work.cuda_stream))
+                rmsd_done[k].record(s_work)
+                if write_centred:
+                    dst = x.ctypes.data + f0 * 12 * A
+                    if host_ok:
+                        check(lib.gbrmsd_write_centred(dst, buf.data_ptr(), 3 * Ap, cent[f0:f0 + n].data_ptr(), n, A,
+                                                       s_work.cuda_stream))
+    except BaseException:
+        # kernels already queued read and write the caller's host array:
+        # let them finish before the error leaves (and the array can go away)
+        s_in.synchronize()
+        s_work.synchronize()
+        raise
     result = np.empty(F, dtype=np.float32)
     copy_rows(result.ctypes.data, 4 * F, out.data_ptr(), 4 * F, 4 * F, 1, 2, s_work.cuda_stream)
     s_work.synchronize()

@@ -538,6 +538,8 @@ StreamCfg choose_cfg(int32_t Ap, bool use_ref) {
 
 int grid_warps(const StreamCfg& c) { return sm_count() * c.warps; }
 
+constexpr int64_t kUnitsPerWarpCap = 4;
+
 // Splits per frame: frames are cut into S units of Q/S quads so that every
 // warp gets work, but each unit also costs a fixed epilogue (shift, warp
 // reduction of 13 compensated sums, record).  S minimises the busiest warp's
@@ -552,9 +554,11 @@ int32_t choose_splits(int64_t F, int32_t Q, int gwarps) {
   if (F <= 0 || gwarps <= 0) return 1;
   int64_t smax = Q / 32;
   if (smax < 1) smax = 1;
-  // beyond ~64 units per warp more splits only add epilogues
-  const int64_t scap = (64LL * gwarps + F - 1) / F;
-  if (smax > scap) smax = scap;
+  // F * S <= max(F, 4 * warps): more than a few units per warp only adds
+  // epilogues, and the cap keeps the record count a monotone bound of F
+  // (rmsd_units_bound)
+  const int64_t scap = (kUnitsPerWarpCap * gwarps) / F;
+  if (smax > scap) smax = scap < 1 ? 1 : scap;
   int32_t best_s = 1;
   double best = 0.0;
   for (int64_t s = 1; s <= smax; ++s) {
@@ -653,10 +657,11 @@ struct WsLayout {
   size_t sums_off, refine_off, cent_off, total;
 };
 
-WsLayout ws_layout(int64_t F, int32_t S) {
+// F frames cut into `units` (frame, split) records
+WsLayout ws_layout(int64_t F, int64_t units) {
   WsLayout w;
   w.sums_off = HDR_BYTES;
-  w.refine_off = align_up(w.sums_off + (size_t)F * S * SUMS_STRIDE * sizeof(double), 256);
+  w.refine_off = align_up(w.sums_off + (size_t)units * SUMS_STRIDE * sizeof(double), 256);
   w.cent_off = align_up(w.refine_off + (size_t)F * sizeof(RefineEntry), 256);
   w.total = align_up(w.cent_off + (size_t)F * 3 * sizeof(float), 256);
   return w;
@@ -688,13 +693,18 @@ int check_frames(const float* x, int64_t F, int32_t A, int32_t Ap, int64_t frame
 
 }  // namespace
 
-// Splits per frame; mode-independent upper bound so one workspace size
-// serves every mode (TRACE uses the same or fewer splits).
-int32_t rmsd_splits_max(int64_t F, int32_t A) {
-  // the largest split count any configuration could choose for this shape
+// Upper bound of F' * S over every call with F' <= F frames, any mode and any
+// launch configuration: choose_splits keeps F' * S <= min(max(F', 4 * warps),
+// F' * Q / 32), which grows with F' and with the warp count, so a workspace
+// sized for F frames also serves every smaller call (the last chunk of a
+// stream, a partial batch).
+int64_t rmsd_units_bound(int64_t F, int32_t A) {
   int gw = 0;
   for (int i = 0; i < kNumCfg; ++i) gw = gw > grid_warps(kCfgs[i]) ? gw : grid_warps(kCfgs[i]);
-  return choose_splits(F, (A + 3) / 4, gw);
+  int64_t smax = ((A + 3) / 4) / 32;
+  if (smax < 1) smax = 1;
+  const int64_t cap = F > kUnitsPerWarpCap * gw ? F : kUnitsPerWarpCap * gw;
+  return F * smax < cap ? F * smax : cap;
 }
 
 // Optional CUDA-event timing of the dominant kernel of each profiled call
@@ -770,13 +780,13 @@ int gbrmsd_reference_info(const void* ref_ws, float* host_trace, float* host_cen
 
 size_t gbrmsd_rotations_workspace_bytes(int64_t n_frames, int32_t n_atoms) {
   if (n_frames < 0 || n_atoms < 0) return 0;
-  return align_up(ws_layout(n_frames, rmsd_splits_max(n_frames, n_atoms)).total, 256) +
+  return align_up(ws_layout(n_frames, rmsd_units_bound(n_frames, n_atoms)).total, 256) +
          align_up((size_t)n_frames * sizeof(float), 256);
 }
 
 size_t gbrmsd_rmsd_workspace_bytes(int64_t n_frames, int32_t n_atoms) {
   if (n_frames < 0 || n_atoms < 0) return 0;
-  return ws_layout(n_frames, rmsd_splits_max(n_frames, n_atoms)).total;
+  return ws_layout(n_frames, rmsd_units_bound(n_frames, n_atoms)).total;
 }
 
 int gbrmsd_rmsd_to_reference(const float* x, int64_t n_frames, int32_t n_atoms, int32_t n_padded,
@@ -803,7 +813,7 @@ int gbrmsd_rmsd_to_reference(const float* x, int64_t n_frames, int32_t n_atoms, 
   }
   const StreamCfg cfg = choose_cfg(n_padded, true);
   const int32_t S = choose_splits(n_frames, (n_atoms + 3) / 4, grid_warps(cfg));
-  const WsLayout L = ws_layout(n_frames, S);
+  const WsLayout L = ws_layout(n_frames, n_frames * S);
   if (!ws || ws_bytes < L.total || !aligned16(ws))
     return set_error(GBRMSD_E_WORKSPACE, "rmsd_to_reference: workspace needs %zu bytes (16-byte aligned)", L.total);
   const RefWsLayout RL = ref_ws_layout(n_atoms, n_padded);
@@ -885,7 +895,7 @@ int gbrmsd_rotations(const float* x, int64_t n_frames, int32_t n_atoms, int32_t 
   if (n_atoms == 0) return set_error(GBRMSD_E_INVALID, "rotations: need at least one alignment atom");
   const StreamCfg cfg = choose_cfg(n_padded, true);
   const int32_t S = choose_splits(n_frames, (n_atoms + 3) / 4, grid_warps(cfg));
-  const WsLayout L = ws_layout(n_frames, S);
+  const WsLayout L = ws_layout(n_frames, n_frames * S);
   const size_t scratch_off = align_up(L.total, 256);
   if (!ws || ws_bytes < scratch_off + align_up((size_t)n_frames * sizeof(float), 256) || !aligned16(ws))
     return set_error(GBRMSD_E_WORKSPACE, "rotations: workspace needs %zu bytes (16-byte aligned)",
@@ -999,7 +1009,7 @@ int gbrmsd_center_inplace(float* x, int64_t n_frames, int32_t n_atoms, int32_t n
   }
   const StreamCfg cfg = choose_cfg(n_padded, false);
   const int32_t S = choose_splits(n_frames, (n_atoms + 3) / 4, grid_warps(cfg));
-  const WsLayout L = ws_layout(n_frames, S);
+  const WsLayout L = ws_layout(n_frames, n_frames * S);
   const size_t need = L.total;
   if (!ws || ws_bytes < need || !aligned16(ws))
     return set_error(GBRMSD_E_WORKSPACE, "center_inplace: workspace needs %zu bytes", need);

@@ -76,3 +76,18 @@ def test_host_side_effect_helper_matches_numpy():
     want = x - c[:, None, :]
     _lib.check(_lib.lib.gbrmsd_host_subtract_centroids(x.ctypes.data, 37, 11, 33, c.ctypes.data, 4))
     np.testing.assert_array_equal(x, want)
+
+
+def test_rmsd_workspace_is_monotone_in_frames():
+    """A workspace sized for F frames must serve every call with fewer frames
+    (the last chunk of a stream, a partial batch): the size never decreases
+    as F grows."""
+    from mdtraj_gb300 import _lib
+
+    lib = _lib.lib
+    for A in (1, 100, 1000, 4000, 10000, 100000):
+        prev = 0
+        for F in list(range(1, 3000, 7)) + [9728, 9729, 10**4, 10**5, 10**6]:
+            w = lib.gbrmsd_rmsd_workspace_bytes(F, A)
+            assert w >= prev, (A, F, w, prev)
+            prev = w

@@ -98,3 +98,16 @@ def test_drop_in_host_side_effect_unaligned_atoms(cuda):
     assert_parity(got, fp64.kabsch_rmsd(x, x[5]), what="drop-in, 33 atoms")
     centred = x.astype(np.float64) - x.astype(np.float64).mean(1, keepdims=True)
     assert np.abs(t.xyz - centred).max() < 2e-6
+
+
+def test_chunked_host_path_small_last_chunk(cuda):
+    """Chunks of 300, 300 and 100 frames of 4,000 atoms: the last chunk uses
+    more splits per frame than the first, inside the workspace sized for the
+    first."""
+    ref, x = synth.single_reference_frames(700, 4000, seed=6, sigma=0.1, exact_fraction=0.01)
+    want = fp64.kabsch_rmsd(x, x[0])
+    ref_dev = D.DeviceReference(x[0], _lib.ATOM_MAJOR, centre=True, device=cuda)
+    host = x.copy()
+    got = D.rmsd_host_frames(host, ref_dev, _lib.MODE_CENTER, self_index=0, write_centred=True,
+                             chunk_bytes=12 * 4000 * 300)
+    assert_parity(got, want, what="chunks of 300/300/100 frames")
