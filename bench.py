@@ -91,8 +91,8 @@ def measured_peaks() -> dict:
 
 def traffic_from_profiles(kernel: str, workload: str):
     """DRAM bytes per launch of `kernel` from a committed ncu summary
-    (profiles/*.txt line: 'dram_bytes_per_launch <kernel> <workload> <bytes>')."""
-    for f in sorted((ROOT / "profiles").glob("*.txt")):
+    (profiles/*.txt or *.md line: 'dram_bytes_per_launch <kernel> <workload> <bytes>')."""
+    for f in sorted((ROOT / "profiles").glob("*.txt")) + sorted((ROOT / "profiles").glob("*.md")):
         for line in f.read_text().splitlines():
             m = re.match(r"dram_bytes_per_launch\s+(\S+)\s+(\S+)\s+([0-9.eE+]+)", line.strip())
             if m and m.group(1) == kernel and m.group(2) == workload:
@@ -1094,7 +1094,7 @@ def run_superpose(args) -> dict:
     peaks = measured_peaks()
     ach = alg / (ms_step / 1e3) / 1e9
     roof = {"bound": "hbm", "achieved": round(ach, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
-            "frac": round(ach / peaks["hbm_gbs"], 4), "traffic": None,
+            "frac": round(ach / peaks["hbm_gbs"], 4), "traffic": traffic_from_profiles("superpose_step", args.workload),
             "kernel": "stream_kernel + finish_kernel + apply_rotations_kernel (whole step)",
             "algorithmic_bytes_per_step": alg,
             "passes_ms": {"rotations": round(ms_rot, 4), "apply": round(ms_apply, 4)},
@@ -1237,7 +1237,8 @@ def run_xtc(args) -> dict:
     moved = float(used + 12.0 * A * F)
     peaks = measured_peaks()
     roof = {"bound": "hbm", "achieved": round(moved / (ms / 1e3) / 1e9, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
-            "frac": round(moved / (ms / 1e3) / 1e9 / peaks["hbm_gbs"], 4), "traffic": None,
+            "frac": round(moved / (ms / 1e3) / 1e9 / peaks["hbm_gbs"], 4),
+            "traffic": traffic_from_profiles("xtc_decode_kernel", "xtc_decode_100000x1001") if F == 100_000 else None,
             "kernel": "xtc_decode_kernel", "kernel_ms": round(ms, 4),
             "algorithmic_bytes_per_launch": moved,
             "note": "compressed bytes read + decoded float32 written; one thread decodes one frame's bit stream "
