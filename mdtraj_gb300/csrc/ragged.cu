@@ -425,6 +425,18 @@ struct RaggedTables {
   size_t ref_total = 0;
 };
 
+// Estimated time of one unit of q quads, in units of a warp's share of HBM
+// per quad (~35 cycles with 16 warps per SM): a unit either streams at that
+// rate, or, when it is small, is held up by its own instructions (~9.4 cycles
+// per quad) plus the per-unit epilogue (shift, warp reduction of 13
+// compensated sums, record: ~3,400 cycles).  Calibrated on single-segment
+// runs: 64-atom frames (16-quad units) stream at 0.93 TB/s, 14% of the copy
+// peak, which this model puts at 16 / (0.27 * 16 + 97) = 16%.
+inline double unit_cost(double q) {
+  const double mem = q, issue = 0.27 * q + 97.0;
+  return mem > issue ? mem : issue;
+}
+
 int build_tables(const int64_t* x_off, const int32_t* atoms, const int32_t* padded, const int64_t* frames, int32_t n,
                  int32_t max_unit_quads, int grid, RaggedTables& t) {
   t.segs.resize(n);
@@ -452,7 +464,7 @@ int build_tables(const int64_t* x_off, const int32_t* atoms, const int32_t* padd
     upf[s] = sp;
     t.total_units += (int64_t)sp * frames[s];
     t.total_frames += frames[s];
-    cost[s] = (double)Q / sp + 24.0;  // per-unit cost in quad equivalents
+    cost[s] = unit_cost((double)Q / sp);
   }
   // contiguous unit ranges of equal cost per CTA
   std::vector<double> seg_cost_prefix(n + 1, 0.0);
