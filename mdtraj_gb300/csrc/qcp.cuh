@@ -128,7 +128,10 @@ __host__ __device__ __forceinline__ double qcp_lambda_max_mixed(const double* m,
   const float a2 = (float)(c2 * inv2);
   const float a1 = (float)(c1 * inv2 * inv);
   const float a0 = (float)(c0 * inv2 * inv2);
-  float x = 1.0f;
+  // start at the tighter of the upper bounds 1 and sqrt(3) |M|_F / lam0 =
+  // sqrt(-1.5 a2) (K is traceless: lambda_max <= sqrt(3/4 tr K^2)), nudged
+  // up by 2^-20 against rounding; Newton from above converges monotonically
+  float x = fminf(1.0f, sqrtf(-1.5f * a2) * 1.00000095f);
   int it = 0;
   for (; it < 40; ++it) {
     const float x2 = x * x;
