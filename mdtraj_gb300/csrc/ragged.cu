@@ -145,6 +145,72 @@ __device__ __forceinline__ void rc_next_unit(RCursor& w, const RaggedArgs& p) {
   rc_enter(w, p);
 }
 
+#ifndef GB_RAGGED_X2
+#define GB_RAGGED_X2 1
+#endif
+
+// Packed float pairs (sm_100+ f32x2 arithmetic): the level-1 sums of a lane
+// run on atom pairs, even atoms in the low half and odd atoms in the high
+// half, so one instruction does the work of two.
+__device__ __forceinline__ uint64_t pk2(float a, float b) {
+  uint64_t r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ float sum2(uint64_t v) {
+  float a, b;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+  return a + b;
+}
+__device__ __forceinline__ uint64_t fma2(uint64_t a, uint64_t b, uint64_t c) {
+  uint64_t d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ uint64_t add2(uint64_t a, uint64_t b) {
+  uint64_t d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+
+// The 13 centred sums of one quad on atom pairs (0, 1) and (2, 3); atoms
+// at or beyond nv (MASKED, the frame's last quad) contribute zeros.
+template <bool MASKED>
+__device__ __forceinline__ void accum_quad_x2(uint64_t (&acc)[13], const float (&ax)[4], const float (&ay)[4],
+                                              const float (&az)[4], const float (&bx)[4], const float (&by)[4],
+                                              const float (&bz)[4], const float (&shift)[3], int nv) {
+#pragma unroll
+  for (int p = 0; p < 2; ++p) {
+    float d[2][3];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int t = 2 * p + h;
+      d[h][0] = ax[t] - shift[0];
+      d[h][1] = ay[t] - shift[1];
+      d[h][2] = az[t] - shift[2];
+      if (MASKED && t >= nv) d[h][0] = d[h][1] = d[h][2] = 0.f;
+    }
+    const uint64_t dx = pk2(d[0][0], d[1][0]), dy = pk2(d[0][1], d[1][1]), dz = pk2(d[0][2], d[1][2]);
+    const uint64_t qx = pk2(bx[2 * p], bx[2 * p + 1]), qy = pk2(by[2 * p], by[2 * p + 1]),
+                   qz = pk2(bz[2 * p], bz[2 * p + 1]);
+    acc[0] = fma2(dx, qx, acc[0]);
+    acc[1] = fma2(dx, qy, acc[1]);
+    acc[2] = fma2(dx, qz, acc[2]);
+    acc[3] = fma2(dy, qx, acc[3]);
+    acc[4] = fma2(dy, qy, acc[4]);
+    acc[5] = fma2(dy, qz, acc[5]);
+    acc[6] = fma2(dz, qx, acc[6]);
+    acc[7] = fma2(dz, qy, acc[7]);
+    acc[8] = fma2(dz, qz, acc[8]);
+    acc[9] = add2(acc[9], dx);
+    acc[10] = add2(acc[10], dy);
+    acc[11] = add2(acc[11], dz);
+    acc[12] = fma2(dx, dx, acc[12]);
+    acc[12] = fma2(dy, dy, acc[12]);
+    acc[12] = fma2(dz, dz, acc[12]);
+  }
+}
+
 // Per-stage description of the staged chunk, written by the issuing lane
 // before its arrive (release) and read by the warp after the wait (acquire).
 struct ChunkMeta {
@@ -213,7 +279,11 @@ __global__ void __launch_bounds__(WARPS * 32, 1) ragged_stream_kernel(const Ragg
   int slot = 0;
   bool failed = false;
   CF acc2[NV];
+#if GB_RAGGED_X2
+  uint64_t acc1[NV];
+#else
   float acc1[NV];
+#endif
   int pending = 0;
   float shift[3] = {0.f, 0.f, 0.f};
 
@@ -228,7 +298,7 @@ __global__ void __launch_bounds__(WARPS * 32, 1) ragged_stream_kernel(const Ragg
     const float* st = reinterpret_cast<const float*>(stages + slot * STAGE_BYTES);
     if (m.flags & 1) {
 #pragma unroll
-      for (int j = 0; j < NV; ++j) { acc2[j] = cf_zero(); acc1[j] = 0.f; }
+      for (int j = 0; j < NV; ++j) { acc2[j] = cf_zero(); acc1[j] = 0; }
       pending = 0;
       float sx = 0.f, sy = 0.f, sz = 0.f, cnt = 0.f;
       if (lane < m.nq) {
@@ -250,10 +320,17 @@ __global__ void __launch_bounds__(WARPS * 32, 1) ragged_stream_kernel(const Ragg
         load_stage_quad<ATOM_MAJOR, CQ>(st, i, ax, ay, az);
         load_ref_quad<ATOM_MAJOR, false>(m.ref, 0, i, bx, by, bz);
         const int nv = m.arem - 4 * i;
+#if GB_RAGGED_X2
+        if (nv < 4)
+          accum_quad_x2<true>(acc1, ax, ay, az, bx, by, bz, shift, nv);
+        else
+          accum_quad_x2<false>(acc1, ax, ay, az, bx, by, bz, shift, 4);
+#else
         if (nv < 4)
           accum_quad<MODE_CENTER, true, NV>(acc1, ax, ay, az, bx, by, bz, shift, nv);
         else
           accum_quad<MODE_CENTER, false, NV>(acc1, ax, ay, az, bx, by, bz, shift, 4);
+#endif
       }
     }
     pending += QPL;
@@ -268,7 +345,11 @@ __global__ void __launch_bounds__(WARPS * 32, 1) ragged_stream_kernel(const Ragg
     const bool unit_end = (m.flags & 2) != 0;
     if (pending >= 4 || unit_end) {
 #pragma unroll
+#if GB_RAGGED_X2
+      for (int j = 0; j < NV; ++j) { cf_add(acc2[j], sum2(acc1[j])); acc1[j] = 0; }
+#else
       for (int j = 0; j < NV; ++j) { cf_add(acc2[j], acc1[j]); acc1[j] = 0.f; }
+#endif
       pending = 0;
     }
     if (unit_end) {
