@@ -319,6 +319,18 @@ int gbrmsd_copy_rows(void* dst, size_t dst_pitch, const void* src, size_t src_pi
  * memory through the host page tables (Grace + NVLink-C2C), else 0. */
 int gbrmsd_pageable_access(void);
 
+/* Page-locks [p, p + bytes) of caller-owned host memory for the device
+ * (cudaHostRegister) / releases it (cudaHostUnregister, p as registered).
+ * The streaming drop-in locks a large host array range by range, ahead of the
+ * kernels that read and write it: on GB300 the GPU then reaches those pages
+ * through its own page tables instead of translating every access through
+ * the host's (measured on a 24 GB array after other processes had streamed
+ * pageable memory: 186-200 ms per md.rmsd locked, 400-1,000 ms unlocked).
+ * Returns GBRMSD_E_UNSUPPORTED (and touches nothing) when the range cannot be
+ * locked, e.g. because the caller has locked it already. */
+int gbrmsd_host_register(void* p, size_t bytes);
+int gbrmsd_host_unregister(void* p);
+
 /* Kernel-based strided row copy: dst row r (dst_pitch floats apart) gets
  * src row r (src_pitch floats apart, row_floats values), then zeros up to
  * dst_fill floats.  Either side may be pageable host memory when

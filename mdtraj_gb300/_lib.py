@@ -79,6 +79,8 @@ SIGNATURES: dict[str, tuple] = {
     "gbrmsd_copy_rows": (C.c_int, [_vp, _sz, _vp, _sz, _sz, _sz, _i32, _vp]),
     "gbrmsd_host_subtract_centroids": (C.c_int, [_vp, _i64, _i32, _i64, _vp, _i32]),
     "gbrmsd_pageable_access": (C.c_int, []),
+    "gbrmsd_host_register": (C.c_int, [_vp, _sz]),
+    "gbrmsd_host_unregister": (C.c_int, [_vp]),
     "gbrmsd_copy_rows_kernel": (C.c_int, [_vp, _i64, _vp, _i64, _i64, _i64, _i64, _vp]),
     "gbrmsd_write_centred": (C.c_int, [_vp, _vp, _i64, _vp, _i64, _i32, _vp]),
 }

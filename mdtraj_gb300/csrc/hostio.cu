@@ -177,6 +177,28 @@ int gbrmsd_pageable_access(void) {
   return (pageable == 1 && uses_pt == 1) ? 1 : 0;
 }
 
+int gbrmsd_host_register(void* p, size_t bytes) {
+  clear_error();
+  if (!p || bytes == 0) return set_error(GBRMSD_E_INVALID, "host_register: null pointer or empty range");
+  const cudaError_t e = cudaHostRegister(p, bytes, cudaHostRegisterDefault);
+  if (e != cudaSuccess) {
+    cudaGetLastError();  // not sticky: the caller continues on pageable access
+    return set_error(GBRMSD_E_UNSUPPORTED, "host_register: %s", cudaGetErrorString(e));
+  }
+  return GBRMSD_OK;
+}
+
+int gbrmsd_host_unregister(void* p) {
+  clear_error();
+  if (!p) return set_error(GBRMSD_E_INVALID, "host_unregister: null pointer");
+  const cudaError_t e = cudaHostUnregister(p);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return set_error(GBRMSD_E_UNSUPPORTED, "host_unregister: %s", cudaGetErrorString(e));
+  }
+  return GBRMSD_OK;
+}
+
 int gbrmsd_copy_rows_kernel(float* dst, int64_t dst_pitch, const float* src, int64_t src_pitch, int64_t row_floats,
                             int64_t dst_fill, int64_t n_rows, void* stream) {
   clear_error();

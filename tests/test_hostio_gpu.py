@@ -111,3 +111,28 @@ def test_chunked_host_path_small_last_chunk(cuda):
     got = D.rmsd_host_frames(host, ref_dev, _lib.MODE_CENTER, self_index=0, write_centred=True,
                              chunk_bytes=12 * 4000 * 300)
     assert_parity(got, want, what="chunks of 300/300/100 frames")
+
+
+def test_host_locks_are_released_and_tolerate_caller_locks(cuda):
+    """The streaming path locks the array range by range and unlocks it
+    before returning; an array the caller locked already is used as is."""
+    A = 100
+    ref, x = synth.single_reference_frames(900, A, seed=12, sigma=0.1)
+    want = fp64.kabsch_rmsd(x, x[3])
+    ref_dev = D.DeviceReference(x[3], _lib.ATOM_MAJOR, centre=True, device=cuda)
+    chunk = 12 * A * 100  # 9 chunks: the array is locked chunk by chunk
+    host = x.copy()
+    got = D.rmsd_host_frames(host, ref_dev, _lib.MODE_CENTER, self_index=3, write_centred=True, chunk_bytes=chunk)
+    assert_parity(got, want, what="locked chunks")
+    # nothing is left locked: the caller can lock the whole array now
+    assert lib.gbrmsd_host_register(host.ctypes.data, host.nbytes) == 0
+    try:
+        again = x.copy()
+        np.copyto(host, again)
+        got2 = D.rmsd_host_frames(host, ref_dev, _lib.MODE_CENTER, self_index=3, write_centred=True,
+                                  chunk_bytes=chunk)
+        assert_parity(got2, want, what="caller-locked array")
+        centred = x.astype(np.float64) - x.astype(np.float64).mean(1, keepdims=True)
+        assert np.abs(host - centred).max() < 2e-6
+    finally:
+        assert lib.gbrmsd_host_unregister(host.ctypes.data) == 0
