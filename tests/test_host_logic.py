@@ -162,6 +162,27 @@ def test_pool_allocator_first_fit_and_merge():
     assert p.free == [(0, 100)] and p.free_rows == 100
 
 
+def test_batch_grouped_by_database_range():
+    """A batch that owns one contiguous run of pool rows is laid out sorted
+    by database range (each request contiguous, the run unchanged); a batch
+    with gaps between its rows is left as admitted."""
+    from mdtraj_gb300.serving import Request, RmsdServer
+
+    def req(q, a, b, p0):
+        r = Request(queries=np.zeros((q, 3, 3), np.float32), db0=a, db1=b)
+        r._p0 = p0
+        return r
+
+    batch = [req(5, 300, 900, 10), req(3, 0, 1000, 15), req(4, 100, 200, 18), req(2, 0, 1000, 22)]
+    RmsdServer._group_by_range(batch)
+    order = sorted(batch, key=lambda r: r._p0)
+    assert [(r.db0, r.db1) for r in order] == [(0, 1000), (0, 1000), (100, 200), (300, 900)]
+    assert [(r._p0, r.n_query) for r in order] == [(10, 3), (13, 2), (15, 4), (19, 5)]
+    gaps = [req(5, 300, 900, 10), req(3, 0, 1000, 40)]
+    RmsdServer._group_by_range(gaps)
+    assert [r._p0 for r in gaps] == [10, 40]
+
+
 def test_cross_request_validation_in_library():
     """gbrmsd_cross_rmsd validates the request table before any device call."""
     import ctypes as C
