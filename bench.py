@@ -877,7 +877,8 @@ def run_serving(args) -> dict:
     torch.cuda.empty_cache()
     setup_s = time.perf_counter() - t_setup
     lib = _lib.lib
-    server = serving.RmsdServer(dbs, method="tensor", query_capacity=16384, hbm_budget_bytes=48 << 30, slots=3)
+    server = serving.RmsdServer(dbs, method="tensor", query_capacity=16384, hbm_budget_bytes=48 << 30, slots=3,
+                                host_pool_bytes=8 << 30)
     base = serving.RmsdServer(dbs, method="fp32", query_capacity=1024, hbm_budget_bytes=48 << 30, slots=1,
                               max_batch_requests=1)
     warm = serving_requests(host_frames, frame_ids, 24, 1e6, 1, max_q, slice_range, F)
@@ -973,6 +974,8 @@ def run_serving(args) -> dict:
                    "query_frames": "log-uniform 1-%d" % max_q, "db_range": "full (50%%) or slice %d-%d" % slice_range,
                    "slots": len(server.slots), "query_capacity": server.qcap, "setup_s": round(setup_s, 1),
                    "latency": "arrival to results in pinned host memory",
+                   "host_result_pool_gb": round(server.hpool.buf.nbytes / 1e9, 1),
+                   "host_result_pool_locked": bool(server.hpool.locked),
                    "l2": "database (%.1f GB prepared) larger than L2; no flush" % (dbs.buf.numel() / 1e9)},
         "sweep": sweep,
         "speedup_at_top_rate": round(top["continuous"]["queries_per_s"] /

@@ -23,8 +23,10 @@ in any mix.  ``slots=1, max_batch_requests=1`` gives one request per launch.
 """
 from __future__ import annotations
 
+import ctypes
 import math
 import time
+import weakref
 from collections import deque
 from dataclasses import dataclass, field
 
@@ -32,6 +34,7 @@ import numpy as np
 import torch
 
 from . import _device as D
+from ._lib import lib
 from .cross import CrossWorkspace, FrameSet, cross_launch, cross_status, request_table
 
 
@@ -53,6 +56,7 @@ class Request:
     _p0: int = field(default=-1, repr=False)
     _out: torch.Tensor | None = field(default=None, repr=False)
     _host: torch.Tensor | None = field(default=None, repr=False)
+    _hoff: int = field(default=-1, repr=False)  # result's page offset in the host result pool
 
     @property
     def n_query(self) -> int:
@@ -100,6 +104,59 @@ class PoolAllocator:
         return sum(ln for _, ln in self.free)
 
 
+class HostResultPool:
+    """Page-locked host memory for request results, handed out in 4 KB pages
+    (first fit) and returned when a result array is dropped.
+
+    Results copied into page-locked memory move by DMA without blocking the
+    host; allocating page-locked memory per request costs far more than the
+    copy (measured on the serving workload: 1,500 requests with ~73 MB
+    results each took 2.9 s of host time in per-request allocations, against
+    0.08 s for everything else).  One numpy buffer is locked once
+    (gbrmsd_host_register) and results are views into it."""
+
+    PAGE = 4096
+
+    def __init__(self, nbytes: int):
+        pages = max(1, int(nbytes) // self.PAGE)
+        self.buf = np.empty(pages * self.PAGE, dtype=np.uint8)
+        self.locked = lib.gbrmsd_host_register(self.buf.ctypes.data, self.buf.nbytes) == 0
+        self.pages = PoolAllocator(pages)
+
+    def take(self, nbytes: int):
+        """Page offset of a free range of nbytes, or None (always None when
+        the buffer could not be page-locked: copies into pageable memory
+        would block the host, so such results get their own locked buffer)."""
+        if not self.locked:
+            return None
+        return self.pages.alloc((int(nbytes) + self.PAGE - 1) // self.PAGE)
+
+    def release(self, off: int, nbytes: int) -> None:
+        self.pages.release(off, (int(nbytes) + self.PAGE - 1) // self.PAGE)
+
+    def ptr(self, off: int) -> int:
+        return self.buf.ctypes.data + off * self.PAGE
+
+    def result(self, off: int, n_floats: int, nbytes: int) -> np.ndarray:
+        """float32 array over the pages at `off`; the pages return to the pool
+        once no array or view of it is left (the array's base is a ctypes
+        object that every view keeps alive)."""
+        holder = (ctypes.c_float * max(1, n_floats)).from_address(self.ptr(off))
+        weakref.finalize(holder, self.release, off, nbytes)
+        return np.frombuffer(holder, dtype=np.float32, count=n_floats)
+
+    def close(self) -> None:
+        if self.locked:
+            lib.gbrmsd_host_unregister(self.buf.ctypes.data)
+            self.locked = False
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class _Slot:
     def __init__(self, device):
         self.stream = torch.cuda.Stream(device=device)
@@ -118,13 +175,16 @@ class RmsdServer:
     hbm_budget_bytes: device bytes for results of admitted requests.
     slots: batches that may be in flight at once (one stream each).
     max_batch_requests: cap on requests per batch (None: no cap).
-    result_to_host: copy each result to pinned host memory (else results stay
-    on the device as tensors).
+    result_to_host: copy each result to page-locked host memory (else results
+    stay on the device as tensors).
+    host_pool_bytes: page-locked host memory for results in flight or held by
+    the caller (HostResultPool); a request whose result does not fit waits
+    for space, or, when nothing is in flight, gets its own page-locked buffer.
     """
 
     def __init__(self, database, *, method: str = "tensor", query_capacity: int = 8192,
                  hbm_budget_bytes: int = 8 << 30, slots: int = 3, max_batch_requests: int | None = None,
-                 result_to_host: bool = True, device=None):
+                 result_to_host: bool = True, host_pool_bytes: int = 4 << 30, device=None):
         self.device = device if device is not None else D.require_device()
         self.db = database if isinstance(database, FrameSet) else FrameSet.from_frames(database, device=self.device)
         self.n_db = self.db.capacity
@@ -139,6 +199,7 @@ class RmsdServer:
         self.slots = [_Slot(self.device) for _ in range(max(1, int(slots)))]
         self.max_batch = max_batch_requests
         self.result_to_host = result_to_host
+        self.hpool = HostResultPool(host_pool_bytes) if result_to_host else None
         self.n_batches = 0
         self.batch_sizes = []
 
@@ -155,12 +216,22 @@ class RmsdServer:
             raise ValueError(f"request {r.rid}: result ({r.result_bytes} bytes) exceeds the HBM budget")
 
     # -- steps of the loop ----------------------------------------------------
-    def _admit(self, r: Request, now: float) -> bool:
+    def _admit(self, r: Request, now: float, idle: bool = False) -> bool:
         if self.used + r.result_bytes > self.budget:
             return False
+        hoff = -1
+        if self.hpool is not None:
+            hoff = self.hpool.take(r.result_bytes)
+            if hoff is None:
+                if self.hpool.locked and not idle:
+                    return False  # wait for results in flight to free host space
+                hoff = -1         # nothing in flight (or no pool): its own locked buffer
         p0 = self.pool.alloc(r.n_query)
         if p0 is None:
+            if hoff >= 0:
+                self.hpool.release(hoff, r.result_bytes)
             return False
+        r._hoff = hoff
         r._p0 = p0
         r._out = torch.empty(r.n_query * (r.db1 - r.db0), dtype=torch.float32, device=self.device)
         self.used += r.result_bytes
@@ -201,8 +272,12 @@ class RmsdServer:
             cross_launch(self.db, self.n_db, self.qset, table, len(batch), self.method, ws, s.cuda_stream)
             if self.result_to_host:
                 for r in batch:
-                    r._host = torch.empty(r._out.numel(), dtype=torch.float32, pin_memory=True)
-                    r._host.copy_(r._out, non_blocking=True)
+                    nb = 4 * r._out.numel()
+                    if r._hoff >= 0:
+                        D.copy_rows(self.hpool.ptr(r._hoff), nb, r._out.data_ptr(), nb, nb, 1, 2, s.cuda_stream)
+                    else:
+                        r._host = torch.empty(r._out.numel(), dtype=torch.float32, pin_memory=True)
+                        r._host.copy_(r._out, non_blocking=True)
             ev = torch.cuda.Event()
             ev.record(s)
         for r in batch:
@@ -217,7 +292,14 @@ class RmsdServer:
         done = slot.batch
         for r in done:
             shape = (r.n_query, r.db1 - r.db0)
-            if keep_results:
+            if self.result_to_host and r._hoff >= 0:
+                if keep_results:
+                    # an array over pool pages; they return when it is dropped
+                    r.result = self.hpool.result(r._hoff, r.n_query * (r.db1 - r.db0), r.result_bytes).reshape(shape)
+                else:
+                    self.hpool.release(r._hoff, r.result_bytes)
+                r._hoff = -1
+            elif keep_results:
                 r.result = (r._host.numpy() if self.result_to_host else r._out).reshape(shape)
             r.refined = refined
             r.t_done = now
@@ -252,8 +334,9 @@ class RmsdServer:
             for slot in self.slots:
                 if slot.event is not None and slot.event.query():
                     finished.extend(self._complete(slot, time.perf_counter() - t0, keep_results))
+            idle = not admitted and all(s.event is None for s in self.slots)
             while queue and (self.max_batch is None or len(admitted) < self.max_batch):
-                if not self._admit(queue[0], now):
+                if not self._admit(queue[0], now, idle=idle and not admitted):
                     break
                 admitted.append(queue.popleft())
             free = [s for s in self.slots if s.event is None]

@@ -162,6 +162,33 @@ def test_pool_allocator_first_fit_and_merge():
     assert p.free == [(0, 100)] and p.free_rows == 100
 
 
+def test_host_result_pool_returns_pages_when_results_are_dropped():
+    """Results are arrays over pool pages; the pages come back only when the
+    result and every view of it are gone (no device needed: without one the
+    pool is simply not page-locked)."""
+    import gc
+
+    from mdtraj_gb300.serving import HostResultPool
+
+    pool = HostResultPool(16 * 4096)
+    pool.locked = True  # (without a device the buffer is not locked; exercise the page bookkeeping)
+    a = pool.take(3 * 4096 + 1)          # 4 pages
+    b = pool.take(4096)                  # 1 page
+    assert (a, b) == (0, 4) and pool.pages.free_rows == 11
+    ra = pool.result(a, 10, 3 * 4096 + 1)
+    ra[:] = np.arange(10, dtype=np.float32)
+    view = ra.reshape(2, 5)[1]
+    del ra
+    gc.collect()
+    assert pool.pages.free_rows == 11 and view.tolist() == [5, 6, 7, 8, 9]
+    del view
+    gc.collect()
+    assert pool.pages.free_rows == 15
+    pool.release(b, 4096)
+    assert pool.pages.free == [(0, 16)]
+    pool.locked = False
+
+
 def test_batch_grouped_by_database_range():
     """A batch that owns one contiguous run of pool rows is laid out sorted
     by database range (each request contiguous, the run unchanged); a batch
