@@ -184,7 +184,7 @@ class RmsdServer:
 
     def __init__(self, database, *, method: str = "tensor", query_capacity: int = 8192,
                  hbm_budget_bytes: int = 8 << 30, slots: int = 3, max_batch_requests: int | None = None,
-                 result_to_host: bool = True, host_pool_bytes: int = 4 << 30, device=None):
+                 result_to_host: bool = True, host_pool_bytes: int = 1 << 30, device=None):
         self.device = device if device is not None else D.require_device()
         self.db = database if isinstance(database, FrameSet) else FrameSet.from_frames(database, device=self.device)
         self.n_db = self.db.capacity
