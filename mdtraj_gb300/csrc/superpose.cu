@@ -117,6 +117,21 @@ __device__ __forceinline__ void rotate(const float* r, float ax, float ay, float
   bz = fmaf(r[6], ax, fmaf(r[7], ay, r[8] * az));
 }
 
+constexpr int RMSF_ILP = 4;  // frames whose loads a thread issues together
+
+// One frame of an atom: d = R x - s (or x - s without a rotation) added to
+// the FP32 partial sums a[0..2] and |d|^2 to a[3].
+__device__ __forceinline__ void rmsf_accum(const float* r, float px, float py, float pz, const float (&s)[3],
+                                           float (&a)[4]) {
+  float bx = px, by = py, bz = pz;
+  if (r) rotate(r, px, py, pz, bx, by, bz);
+  const float dx = bx - s[0], dy = by - s[1], dz = bz - s[2];
+  a[0] += dx;
+  a[1] += dy;
+  a[2] += dz;
+  a[3] = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, a[3])));
+}
+
 // part[(chunk * A + k) * 4 + {0,1,2,3}] = sums over the chunk's frames of
 // d = R_f x_fk - s_k (3 components) and |d|^2, s_k = R_0 x_0k.
 __global__ void __launch_bounds__(RMSF_THREADS) rmsf_partial_kernel(const float* __restrict__ x, int64_t F, int32_t A,
@@ -141,15 +156,27 @@ __global__ void __launch_bounds__(RMSF_THREADS) rmsf_partial_kernel(const float*
     __syncthreads();
     float a[4] = {0.f, 0.f, 0.f, 0.f};
     if (k < A) {
-      for (int i = 0; i < nf; ++i) {
+      // frames in groups of RMSF_ILP: all their loads are issued before any
+      // is used, so a thread keeps RMSF_ILP frames in flight (one at a time
+      // left the pass latency-bound at ~4 TB/s); the sums still run in frame
+      // order, so the results do not change
+      int i = 0;
+      for (; i + RMSF_ILP <= nf; i += RMSF_ILP) {
+        float px[RMSF_ILP], py[RMSF_ILP], pz[RMSF_ILP];
+#pragma unroll
+        for (int u = 0; u < RMSF_ILP; ++u) {
+          const float* p = x + (fb + i + u) * fs + 3 * (int64_t)k;
+          px[u] = p[0];
+          py[u] = p[1];
+          pz[u] = p[2];
+        }
+#pragma unroll
+        for (int u = 0; u < RMSF_ILP; ++u)
+          rmsf_accum(rot ? sr + 9 * (i + u) : nullptr, px[u], py[u], pz[u], s, a);
+      }
+      for (; i < nf; ++i) {
         const float* p = x + (fb + i) * fs + 3 * (int64_t)k;
-        float bx = p[0], by = p[1], bz = p[2];
-        if (rot) rotate(sr + 9 * i, p[0], p[1], p[2], bx, by, bz);
-        const float dx = bx - s[0], dy = by - s[1], dz = bz - s[2];
-        a[0] += dx;
-        a[1] += dy;
-        a[2] += dz;
-        a[3] = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, a[3])));
+        rmsf_accum(rot ? sr + 9 * i : nullptr, p[0], p[1], p[2], s, a);
       }
     }
 #pragma unroll
