@@ -878,7 +878,7 @@ def run_serving(args) -> dict:
     setup_s = time.perf_counter() - t_setup
     lib = _lib.lib
     server = serving.RmsdServer(dbs, method="tensor", query_capacity=16384, hbm_budget_bytes=48 << 30, slots=3,
-                                host_pool_bytes=8 << 30)
+                                host_pool_bytes=4 << 30)
     base = serving.RmsdServer(dbs, method="fp32", query_capacity=1024, hbm_budget_bytes=48 << 30, slots=1,
                               max_batch_requests=1)
     warm = serving_requests(host_frames, frame_ids, 24, 1e6, 1, max_q, slice_range, F)
