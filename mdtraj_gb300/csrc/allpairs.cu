@@ -375,7 +375,8 @@ int launch_allpairs_tc(const __nv_bfloat16* Xhi, const __nv_bfloat16* Xlo, const
 int launch_cross_tc(const __nv_bfloat16* Ahi, const __nv_bfloat16* Alo, const double* Ga, int64_t n_a, int64_t cap_a,
                     const __nv_bfloat16* Bhi, const __nv_bfloat16* Blo, const double* Gb, int64_t cap_b, int32_t A,
                     int32_t kpad, const gbrmsd_cross_request_t* reqs, const int32_t* colreq, const int2* tiles,
-                    int64_t n_tiles, PairRefine* rl, int* rc, int rcap, int* err, cudaStream_t st);
+                    int64_t max_tiles, const int64_t* n_tiles_dev, PairRefine* rl, int* rc, int rcap, int* err,
+                    cudaStream_t st);
 int cross_tc_block_frames(int* rows, int* cols);
 
 namespace {
@@ -400,7 +401,7 @@ FsLayout fs_layout(int64_t cap, int32_t A) {
 
 // Cross workspace: [header | requests | column -> request | tiles | refinement list].
 struct CrossWs {
-  size_t reqs, colreq, tiles, rl, total;
+  size_t reqs, colreq, tiles, rl, act, cnt, ntl, total;
   int64_t max_tiles;
   int rcap;
 };
@@ -418,18 +419,34 @@ CrossWs cross_ws(int64_t n_db, int64_t qcap, int32_t n_req) {
   w.rl = align_up(w.tiles + (size_t)w.max_tiles * sizeof(int2), 256);
   const int64_t pairs = n_db * qcap;
   w.rcap = (int)(pairs < (1 << 22) ? (pairs > 0 ? pairs : 1) : (1 << 22));
-  w.total = align_up(w.rl + (size_t)w.rcap * sizeof(PairRefine), 256);
+  // device tile builder: active column blocks (16 B each), per-row-block
+  // counts / offsets, tile count
+  w.act = align_up(w.rl + (size_t)w.rcap * sizeof(PairRefine), 256);
+  w.cnt = align_up(w.act + (size_t)ceil_div(qcap, fn) * 16, 256);
+  w.ntl = align_up(w.cnt + (size_t)(ceil_div(n_db, fm) + 1) * sizeof(int64_t), 256);
+  w.total = align_up(w.ntl + sizeof(int64_t), 256);
   return w;
 }
 
-// Validates the requests, fills the column -> request map and lists the
-// (row block, column block) tiles that hold at least one requested pair:
-// per column block, the row blocks between the lowest and highest database
-// frame its requests ask for; row-block-major so that CTAs running at the same
-// time share database rows in L2.
-int build_cross_tiles(const gbrmsd_cross_request_t* reqs, int32_t n_req, int64_t n_db, int64_t qcap, int fr_rows,
-                      int fr_cols, std::vector<int2>& tiles, std::vector<int32_t>& colreq) {
-  colreq.assign((size_t)qcap, -1);
+// Column blocks of a cross call that hold requested pairs, with the row
+// blocks between the lowest and highest database frame their requests ask
+// for (inclusive).
+struct ActiveBlock {
+  int32_t cb, lo, hi, pad;
+};
+
+struct CrossColumns {
+  std::vector<int32_t> colreq;      // query row -> request (-1: none)
+  std::vector<ActiveBlock> active;  // ascending column block
+  int64_t rmin = 0, n_rb = 0;       // row blocks [rmin, rmin + n_rb)
+  int64_t max_tiles = 0;            // n_rb * active.size(): an upper bound of the tile count
+};
+
+// Validates the requests and fills the column -> request map and the active
+// column blocks.
+int build_cross_columns(const gbrmsd_cross_request_t* reqs, int32_t n_req, int64_t n_db, int64_t qcap, int fr_rows,
+                        int fr_cols, CrossColumns& cc) {
+  cc.colreq.assign((size_t)qcap, -1);
   const int64_t ncb = ceil_div(qcap, fr_cols);
   std::vector<int64_t> lo((size_t)ncb, INT64_MAX), hi((size_t)ncb, -1);
   for (int32_t r = 0; r < n_req; ++r) {
@@ -442,9 +459,10 @@ int build_cross_tiles(const gbrmsd_cross_request_t* reqs, int32_t n_req, int64_t
     if (q.n_query == 0 || q.db1 == q.db0) continue;
     if (!q.out) return set_error(GBRMSD_E_INVALID, "cross: request %d has no output buffer", r);
     for (int64_t j = q.pool0; j < q.pool0 + q.n_query; ++j) {
-      if (colreq[(size_t)j] >= 0) return set_error(GBRMSD_E_INVALID, "cross: requests %d and %d share query row %lld",
-                                                   colreq[(size_t)j], r, (long long)j);
-      colreq[(size_t)j] = r;
+      if (cc.colreq[(size_t)j] >= 0)
+        return set_error(GBRMSD_E_INVALID, "cross: requests %d and %d share query row %lld", cc.colreq[(size_t)j], r,
+                         (long long)j);
+      cc.colreq[(size_t)j] = r;
     }
     const int64_t rb0 = q.db0 / fr_rows, rb1 = (q.db1 - 1) / fr_rows;
     for (int64_t cb = q.pool0 / fr_cols; cb <= (q.pool0 + q.n_query - 1) / fr_cols; ++cb) {
@@ -452,19 +470,78 @@ int build_cross_tiles(const gbrmsd_cross_request_t* reqs, int32_t n_req, int64_t
       hi[(size_t)cb] = std::max(hi[(size_t)cb], rb1);
     }
   }
-  std::vector<int32_t> active;
+  cc.active.clear();
   int64_t rmin = INT64_MAX, rmax = -1;
   for (int64_t cb = 0; cb < ncb; ++cb)
     if (hi[(size_t)cb] >= 0) {
-      active.push_back((int32_t)cb);
+      cc.active.push_back(ActiveBlock{(int32_t)cb, (int32_t)lo[(size_t)cb], (int32_t)hi[(size_t)cb], 0});
       rmin = std::min(rmin, lo[(size_t)cb]);
       rmax = std::max(rmax, hi[(size_t)cb]);
     }
-  tiles.clear();
-  for (int64_t rb = rmin; rb <= rmax; ++rb)
-    for (int32_t cb : active)
-      if (rb >= lo[(size_t)cb] && rb <= hi[(size_t)cb]) tiles.push_back(make_int2((int)rb, cb));
+  cc.rmin = cc.active.empty() ? 0 : rmin;
+  cc.n_rb = cc.active.empty() ? 0 : rmax - rmin + 1;
+  cc.max_tiles = cc.n_rb * (int64_t)cc.active.size();
   return GBRMSD_OK;
+}
+
+// The (row block, column block) tiles that hold at least one requested pair,
+// row-block-major so that CTAs running at the same time share database rows
+// in L2.  Host version, for the FP32 tiles (whose grid is one CTA per tile).
+void host_cross_tiles(const CrossColumns& cc, std::vector<int2>& tiles) {
+  tiles.clear();
+  for (int64_t i = 0; i < cc.n_rb; ++i) {
+    const int64_t rb = cc.rmin + i;
+    for (const ActiveBlock& b : cc.active)
+      if (rb >= b.lo && rb <= b.hi) tiles.push_back(make_int2((int)rb, b.cb));
+  }
+}
+
+// The same list built on the device (tensor path), so that neither the host
+// loop over up to millions of tiles nor their pageable upload holds the host
+// up: count the tiles of every row block, scan the counts, write each row
+// block's tiles at its offset.  Same order as host_cross_tiles.
+__global__ void __launch_bounds__(256) cross_tile_count_kernel(const ActiveBlock* __restrict__ act, int32_t n_act,
+                                                              int64_t rmin, int64_t n_rb, int64_t* __restrict__ cnt) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_rb; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t rb = rmin + i;
+    int64_t c = 0;
+    for (int32_t k = 0; k < n_act; ++k) c += (rb >= act[k].lo && rb <= act[k].hi) ? 1 : 0;
+    cnt[i] = c;
+  }
+}
+
+// In-place exclusive scan of cnt[0, n) by one block; *total = the sum.
+__global__ void __launch_bounds__(1024) cross_tile_scan_kernel(int64_t* __restrict__ cnt, int64_t n,
+                                                              int64_t* __restrict__ total) {
+  __shared__ int64_t part[1024];
+  int64_t carry = 0;
+  for (int64_t base = 0; base < n; base += 1024) {
+    const int64_t i = base + threadIdx.x;
+    const int64_t v = i < n ? cnt[i] : 0;
+    part[threadIdx.x] = v;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+      const int64_t t = threadIdx.x >= (unsigned)off ? part[threadIdx.x - off] : 0;
+      __syncthreads();
+      part[threadIdx.x] += t;
+      __syncthreads();
+    }
+    if (i < n) cnt[i] = carry + part[threadIdx.x] - v;
+    carry += part[1023];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void __launch_bounds__(256) cross_tile_fill_kernel(const ActiveBlock* __restrict__ act, int32_t n_act,
+                                                             int64_t rmin, int64_t n_rb, const int64_t* __restrict__ off,
+                                                             int2* __restrict__ tiles) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_rb; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t rb = rmin + i;
+    int64_t p = off[i];
+    for (int32_t k = 0; k < n_act; ++k)
+      if (rb >= act[k].lo && rb <= act[k].hi) tiles[p++] = make_int2((int)rb, act[k].cb);
+  }
 }
 
 }  // namespace
@@ -615,25 +692,42 @@ int gbrmsd_cross_rmsd(const void* db_set, int64_t db_capacity, int64_t n_db, con
     return set_error(GBRMSD_E_WORKSPACE, "cross: workspace needs %zu bytes", W.total);
   int fm = TBF, fn = TBF;
   if (method == 1) cross_tc_block_frames(&fm, &fn);
-  std::vector<int2> tiles;
-  std::vector<int32_t> colreq;
-  int rc = build_cross_tiles(requests, n_requests, n_db, query_capacity, fm, fn, tiles, colreq);
+  CrossColumns cc;
+  int rc = build_cross_columns(requests, n_requests, n_db, query_capacity, fm, fn, cc);
   if (rc) return rc;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   unsigned char* w = static_cast<unsigned char*>(ws);
   int* hdr = reinterpret_cast<int*>(w);
   GB_CUDA_TRY(cudaMemsetAsync(hdr, 0, 8, st), "memset cross header");
-  if (tiles.empty()) return GBRMSD_OK;
+  if (cc.max_tiles == 0) return GBRMSD_OK;
   auto* dreq = reinterpret_cast<gbrmsd_cross_request_t*>(w + W.reqs);
   auto* dcol = reinterpret_cast<int32_t*>(w + W.colreq);
   auto* dtiles = reinterpret_cast<int2*>(w + W.tiles);
   auto* rl = reinterpret_cast<PairRefine*>(w + W.rl);
   GB_CUDA_TRY(cudaMemcpyAsync(dreq, requests, sizeof(gbrmsd_cross_request_t) * n_requests, cudaMemcpyHostToDevice, st),
               "upload cross requests");
-  GB_CUDA_TRY(cudaMemcpyAsync(dcol, colreq.data(), sizeof(int32_t) * colreq.size(), cudaMemcpyHostToDevice, st),
+  GB_CUDA_TRY(cudaMemcpyAsync(dcol, cc.colreq.data(), sizeof(int32_t) * cc.colreq.size(), cudaMemcpyHostToDevice, st),
               "upload column map");
-  GB_CUDA_TRY(cudaMemcpyAsync(dtiles, tiles.data(), sizeof(int2) * tiles.size(), cudaMemcpyHostToDevice, st),
-              "upload cross tiles");
+  std::vector<int2> tiles;  // host tile list (FP32 tiles only)
+  int64_t* d_ntl = nullptr;
+  if (method == 0) {
+    host_cross_tiles(cc, tiles);
+    GB_CUDA_TRY(cudaMemcpyAsync(dtiles, tiles.data(), sizeof(int2) * tiles.size(), cudaMemcpyHostToDevice, st),
+                "upload cross tiles");
+  } else {
+    auto* dact = reinterpret_cast<ActiveBlock*>(w + W.act);
+    auto* dcnt = reinterpret_cast<int64_t*>(w + W.cnt);
+    d_ntl = reinterpret_cast<int64_t*>(w + W.ntl);
+    GB_CUDA_TRY(cudaMemcpyAsync(dact, cc.active.data(), sizeof(ActiveBlock) * cc.active.size(), cudaMemcpyHostToDevice,
+                                st),
+                "upload active column blocks");
+    const int32_t n_act = (int32_t)cc.active.size();
+    const int blocks = (int)std::min<int64_t>(ceil_div(cc.n_rb, 256), (int64_t)sm_count() * 4);
+    cross_tile_count_kernel<<<blocks, 256, 0, st>>>(dact, n_act, cc.rmin, cc.n_rb, dcnt);
+    cross_tile_scan_kernel<<<1, 1024, 0, st>>>(dcnt, cc.n_rb, d_ntl);
+    cross_tile_fill_kernel<<<blocks, 256, 0, st>>>(dact, n_act, cc.rmin, cc.n_rb, dcnt, dtiles);
+    GB_CUDA_TRY(cudaGetLastError(), "launch cross tile builder");
+  }
   const FsLayout La = fs_layout(db_capacity, n_atoms), Lb = fs_layout(query_capacity, n_atoms);
   const unsigned char* a = static_cast<const unsigned char*>(db_set);
   const unsigned char* b = static_cast<const unsigned char*>(query_set);
@@ -671,7 +765,7 @@ int gbrmsd_cross_rmsd(const void* db_set, int64_t db_capacity, int64_t n_db, con
     rc = launch_cross_tc(reinterpret_cast<const __nv_bfloat16*>(a + La.hi), reinterpret_cast<const __nv_bfloat16*>(a + La.lo),
                          Ga, n_db, db_capacity, reinterpret_cast<const __nv_bfloat16*>(b + Lb.hi),
                          reinterpret_cast<const __nv_bfloat16*>(b + Lb.lo), Gb, query_capacity, n_atoms, La.kpad, dreq,
-                         dcol, dtiles, (int64_t)tiles.size(), rl, hdr + 1, W.rcap, hdr, st);
+                         dcol, dtiles, cc.max_tiles, d_ntl, rl, hdr + 1, W.rcap, hdr, st);
     if (rc) return rc;
     prof_end(st);
   }

@@ -89,7 +89,8 @@ constexpr int SMEM_TOTAL = SMEM_COLV + FR_N * (int)sizeof(CrossCol) + 1024;  // 
 struct TcArgs {
   const double* G;    // traces of the row frames
   const int2* tiles;  // (row block, column block)
-  int64_t n_tiles;
+  int64_t n_tiles;    // tile count, or an upper bound of it when n_tiles_dev is set
+  const int64_t* n_tiles_dev;  // tile count written by an earlier kernel on the stream (cross calls)
   int64_t F;          // row frames (all-pairs: also the column frames)
   int32_t A;
   int32_t kpad;
@@ -256,7 +257,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) allpairs_tc_kernel(const __grid_c
   tc_fence_after();
   const uint32_t tmem_base = *tmem_slot;
 
-  const int64_t n_tiles = args.n_tiles;
+  const int64_t n_tiles = args.n_tiles_dev ? *args.n_tiles_dev : args.n_tiles;
   const int nkb = args.kpad / KBLK;
   const int nunit = (nkb + KFOLD - 1) / KFOLD;
 
@@ -527,6 +528,7 @@ int launch_allpairs_tc(const __nv_bfloat16* Xhi, const __nv_bfloat16* Xlo, const
   a.G = G;
   a.tiles = dtiles;
   a.n_tiles = (int64_t)tiles.size();
+  a.n_tiles_dev = nullptr;
   a.F = F;
   a.A = A;
   a.kpad = kpad;
@@ -552,10 +554,12 @@ int launch_allpairs_tc(const __nv_bfloat16* Xhi, const __nv_bfloat16* Xlo, const
 int launch_cross_tc(const __nv_bfloat16* Ahi, const __nv_bfloat16* Alo, const double* Ga, int64_t n_a, int64_t cap_a,
                     const __nv_bfloat16* Bhi, const __nv_bfloat16* Blo, const double* Gb, int64_t cap_b, int32_t A,
                     int32_t kpad, const gbrmsd_cross_request_t* reqs, const int32_t* colreq, const int2* tiles,
-                    int64_t n_tiles, PairRefine* rl, int* rc, int rcap, int* err, cudaStream_t st) {
+                    int64_t max_tiles, const int64_t* n_tiles_dev, PairRefine* rl, int* rc, int rcap, int* err,
+                    cudaStream_t st) {
   if (kpad % KBLK) return set_error(GBRMSD_E_INVALID, "cross_tc: k padding must be a multiple of 64");
   if (max_dyn_smem() < SMEM_TOTAL) return set_error(GBRMSD_E_UNSUPPORTED, "cross_tc: not enough shared memory");
-  if (n_tiles == 0) return GBRMSD_OK;
+  if (max_tiles == 0) return GBRMSD_OK;
+  const int64_t n_tiles = max_tiles;
   alignas(64) CUtensorMap mha, mla, mhb, mlb;
   memset(&mha, 0, sizeof(mha));
   memset(&mla, 0, sizeof(mla));
@@ -570,6 +574,7 @@ int launch_cross_tc(const __nv_bfloat16* Ahi, const __nv_bfloat16* Alo, const do
   a.G = Ga;
   a.tiles = tiles;
   a.n_tiles = n_tiles;
+  a.n_tiles_dev = n_tiles_dev;
   a.F = n_a;
   a.A = A;
   a.kpad = kpad;
