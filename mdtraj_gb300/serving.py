@@ -34,7 +34,7 @@ import numpy as np
 import torch
 
 from . import _device as D
-from ._lib import check, lib
+from ._lib import lib
 from .cross import CrossWorkspace, FrameSet, cross_launch, cross_status, request_table
 
 
@@ -57,7 +57,6 @@ class Request:
     _out: torch.Tensor | None = field(default=None, repr=False)
     _host: torch.Tensor | None = field(default=None, repr=False)
     _hoff: int = field(default=-1, repr=False)  # result's page offset in the host result pool
-    _qhost: np.ndarray | None = field(default=None, repr=False)  # queries read by the upload kernel
 
     @property
     def n_query(self) -> int:
@@ -264,18 +263,9 @@ class RmsdServer:
         self._group_by_range(batch)
         s = slot.stream
         with torch.cuda.stream(s):
-            pageable = D.pageable_access()
             for r in batch:
                 rows = self.staging[r._p0:r._p0 + r.n_query]
-                if pageable:
-                    # a copy kernel reads the request's numpy queries: the host
-                    # does not wait behind result copies on the copy engines
-                    r._qhost = np.ascontiguousarray(r.queries, dtype=np.float32)
-                    n = 3 * self.n_atoms
-                    check(lib.gbrmsd_copy_rows_kernel(rows.data_ptr(), n, r._qhost.ctypes.data, n, n, n, r.n_query,
-                                                      s.cuda_stream))
-                else:
-                    rows.copy_(torch.from_numpy(r.queries.reshape(r.n_query, -1)), non_blocking=True)
+                rows.copy_(torch.from_numpy(r.queries.reshape(r.n_query, -1)), non_blocking=True)
                 self.qset.prepare(rows, r._p0, stream=s.cuda_stream)
             table = request_table([(r._out.data_ptr(), r._p0, r.n_query, r.db0, r.db1) for r in batch])
             ws = slot.ws.get(self.n_db, self.qcap, len(batch))
@@ -313,7 +303,6 @@ class RmsdServer:
                 r.result = (r._host.numpy() if self.result_to_host else r._out).reshape(shape)
             r.refined = refined
             r.t_done = now
-            r._qhost = None
             self.pool.release(r._p0, r.n_query)
             self.used -= r.result_bytes
             r._out = None if self.result_to_host or not keep_results else r._out
