@@ -90,6 +90,23 @@ def test_chunked_host_path_matches_oracle(cuda, chunk_bytes):
     assert np.abs(host - centred).max() < 2e-6
 
 
+def test_one_chunk_array_goes_as_two_halves(cuda, monkeypatch):
+    """An array that fits one chunk but is above the two-halves threshold
+    (lowered here) streams as two halves of 151 and 150 frames, self frame
+    in the second half: the same RMSDs and the same in-place centring."""
+    monkeypatch.setattr(D, "TWO_CHUNK_MIN_BYTES", 1)
+    A = 24
+    ref, x = synth.single_reference_frames(301, A, seed=22, sigma=0.2, exact_fraction=0.02)
+    want = fp64.kabsch_rmsd(x, x[200])
+    ref_dev = D.DeviceReference(x[200], _lib.ATOM_MAJOR, centre=True, device=cuda)
+    host = x.copy()
+    got = D.rmsd_host_frames(host, ref_dev, _lib.MODE_CENTER, self_index=200, write_centred=True)
+    assert got[200] == 0.0
+    assert_parity(got, want, what="two halves")
+    centred = x.astype(np.float64) - x.astype(np.float64).mean(1, keepdims=True)
+    assert np.abs(host - centred).max() < 2e-6
+
+
 def test_drop_in_host_side_effect_unaligned_atoms(cuda):
     """The drop-in on an array whose rows are not a multiple of 16 bytes."""
     ref, x = synth.single_reference_frames(120, 33, seed=4, sigma=0.1)
