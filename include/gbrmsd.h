@@ -9,6 +9,12 @@
  * GBRMSD_OK (0) on success and a negative GBRMSD_E_* code on failure, with a
  * message available from gbrmsd_last_error() (thread-local).
  *
+ * Threads: the compute entry points may be called from several host threads
+ * at once (mdtraj runs its kernels with the GIL released), each call with its
+ * own workspace and normally its own stream; the library keeps no per-call
+ * state anywhere else.  gbrmsd_stream_config_select and the gbrmsd_profile_*
+ * calls change process-wide settings and must not race with other calls.
+ *
  * Coordinates are float32 nanometres in one of two padded layouts:
  *   GBRMSD_ATOM_MAJOR  frame f, atom k, axis c at x[f*frame_stride + 3*k + c]
  *   GBRMSD_AXIS_MAJOR  frame f, axis c, atom k at x[f*frame_stride + c*n_padded + k]

@@ -464,16 +464,20 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
+EncodeTiledFn lookup_encode_tiled() {
+  void* p = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess)
+    return nullptr;
+  return reinterpret_cast<EncodeTiledFn>(p);
+}
+
 int encode_plane(CUtensorMap* tm, const void* base, int64_t rows, int32_t kpad, int box_rows) {
-  static EncodeTiledFn fn = nullptr;
-  if (!fn) {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    GB_CUDA_TRY(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q),
-                "cudaGetDriverEntryPointByVersion(cuTensorMapEncodeTiled)");
-    if (q != cudaDriverEntryPointSuccess || !p) return set_error(GBRMSD_E_UNSUPPORTED, "cuTensorMapEncodeTiled missing");
-    fn = reinterpret_cast<EncodeTiledFn>(p);
-  }
+  // looked up once per process (a function-local static is initialised
+  // exactly once even when host threads call concurrently)
+  static const EncodeTiledFn fn = lookup_encode_tiled();
+  if (!fn) return set_error(GBRMSD_E_UNSUPPORTED, "cuTensorMapEncodeTiled is not available");
   const cuuint64_t dims[2] = {(cuuint64_t)kpad, (cuuint64_t)rows};
   const cuuint64_t strides[1] = {(cuuint64_t)kpad * 2};
   const cuuint32_t box[2] = {KBLK, (cuuint32_t)box_rows};

@@ -2,6 +2,7 @@
 #include <stdarg.h>
 #include <stdio.h>
 
+#include <atomic>
 #include <thread>
 #include <vector>
 
@@ -12,9 +13,12 @@ namespace gb {
 namespace {
 thread_local char g_last_error[1024] = "";
 
+// Per-device attributes, filled on first use.  Host threads may race on the
+// first fill: both store the same values, smem before sm, and a reader that
+// sees sm != 0 (acquire) also sees smem.
 struct DevCache {
-  int sm = 0;
-  int smem = 0;
+  std::atomic<int> sm{0};
+  std::atomic<int> smem{0};
 };
 DevCache g_dev[64];
 }  // namespace
@@ -37,16 +41,18 @@ static DevCache& dev_cache() {
   int d = 0;
   cudaGetDevice(&d);
   DevCache& c = g_dev[(d >= 0 && d < 64) ? d : 0];
-  if (c.sm == 0) {
-    cudaDeviceGetAttribute(&c.sm, cudaDevAttrMultiProcessorCount, d);
-    cudaDeviceGetAttribute(&c.smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, d);
-    if (c.sm <= 0) c.sm = 1;
+  if (c.sm.load(std::memory_order_acquire) == 0) {
+    int sm = 0, smem = 0;
+    cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, d);
+    cudaDeviceGetAttribute(&smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, d);
+    c.smem.store(smem, std::memory_order_relaxed);
+    c.sm.store(sm > 0 ? sm : 1, std::memory_order_release);
   }
   return c;
 }
 
-int sm_count() { return dev_cache().sm; }
-int max_dyn_smem() { return dev_cache().smem; }
+int sm_count() { return dev_cache().sm.load(std::memory_order_relaxed); }
+int max_dyn_smem() { return dev_cache().smem.load(std::memory_order_relaxed); }
 
 }  // namespace gb
 

@@ -31,6 +31,8 @@
 #include <math.h>
 #include <string.h>
 
+#include <atomic>
+
 #include "capi_internal.h"
 #include "common.cuh"
 #include "qcp.cuh"
@@ -616,17 +618,20 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
+EncodeTiledFn lookup_encode_tiled() {
+  void* p = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess)
+    return nullptr;
+  return reinterpret_cast<EncodeTiledFn>(p);
+}
+
 int encode_axis_map(CUtensorMap* tm, const StreamArgs& a) {
-  static EncodeTiledFn fn = nullptr;
-  if (!fn) {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    GB_CUDA_TRY(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q),
-                "cudaGetDriverEntryPointByVersion(cuTensorMapEncodeTiled)");
-    if (q != cudaDriverEntryPointSuccess || !p)
-      return set_error(GBRMSD_E_UNSUPPORTED, "cuTensorMapEncodeTiled is not available");
-    fn = reinterpret_cast<EncodeTiledFn>(p);
-  }
+  // looked up once per process (a function-local static is initialised
+  // exactly once even when host threads call concurrently)
+  static const EncodeTiledFn fn = lookup_encode_tiled();
+  if (!fn) return set_error(GBRMSD_E_UNSUPPORTED, "cuTensorMapEncodeTiled is not available");
   // (atoms, axes, frames); box = 256 atoms x 3 axes x 1 frame
   const cuuint64_t dims[3] = {(cuuint64_t)a.n_padded, 3, (cuuint64_t)a.n_frames};
   const cuuint64_t strides[2] = {(cuuint64_t)a.n_padded * 4, (cuuint64_t)a.frame_stride * 4};
@@ -736,7 +741,7 @@ void prof_end(cudaStream_t st) {
 // to 65,536 frames of any atom count on a 152-SM GB300.
 constexpr size_t kNoallocScratchBytes = 16u << 20;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
-static void* g_noalloc_scratch_addr[64] = {};
+static std::atomic<void*> g_noalloc_scratch_addr[64] = {};
 
 using namespace gb;
 
@@ -974,11 +979,11 @@ int gbrmsd_rmsd_to_reference_noalloc(const float* x, int64_t n_frames, int32_t n
   int dev = 0;
   GB_CUDA_TRY(cudaGetDevice(&dev), "cudaGetDevice");
   if (dev < 0 || dev >= 64) return set_error(GBRMSD_E_UNSUPPORTED, "rmsd_to_reference_noalloc: device %d", dev);
-  if (!g_noalloc_scratch_addr[dev]) {
-    void* p = nullptr;
-    GB_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress(g_noalloc_scratch)");
-    if (!p) return set_error(GBRMSD_E_CUDA, "rmsd_to_reference_noalloc: null scratch address");
-    g_noalloc_scratch_addr[dev] = p;
+  void* scratch = g_noalloc_scratch_addr[dev].load(std::memory_order_acquire);
+  if (!scratch) {
+    GB_CUDA_TRY(cudaGetSymbolAddress(&scratch, g_noalloc_scratch), "cudaGetSymbolAddress(g_noalloc_scratch)");
+    if (!scratch) return set_error(GBRMSD_E_CUDA, "rmsd_to_reference_noalloc: null scratch address");
+    g_noalloc_scratch_addr[dev].store(scratch, std::memory_order_release);
   }
   if (n_frames < 0 || n_atoms < 0) return set_error(GBRMSD_E_INVALID, "negative n_frames/n_atoms");
   const size_t need = gbrmsd_rmsd_workspace_bytes(n_frames, n_atoms);
@@ -989,7 +994,7 @@ int gbrmsd_rmsd_to_reference_noalloc(const float* x, int64_t n_frames, int32_t n
                      "gbrmsd_rmsd_to_reference with a workspace",
                      (long long)n_frames, n_atoms, need, kNoallocScratchBytes);
   return gbrmsd_rmsd_to_reference(x, n_frames, n_atoms, n_padded, frame_stride, layout, mode, ref_ws, g_target,
-                                  g_ref, self_index, out_rmsd, out_centroid, out_trace, g_noalloc_scratch_addr[dev],
+                                  g_ref, self_index, out_rmsd, out_centroid, out_trace, scratch,
                                   kNoallocScratchBytes, stream);
 }
 
