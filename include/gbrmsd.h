@@ -104,8 +104,10 @@ int gbrmsd_rmsd_to_reference(const float* x, int64_t n_frames, int32_t n_atoms, 
 /* Allocation-free variant of gbrmsd_rmsd_to_reference.  It has no
  * counterpart in the reference (mdtraj's CPU path never allocates device
  * memory).  For callers that cannot allocate device memory at the point they
- * need RMSDs -- code running during CUDA-graph capture, inside another
- * runtime's memory pool, or a plugin without an allocator -- the scratch is a
+ * need RMSDs -- code inside another runtime's memory pool (the pool owns the
+ * device memory), a plugin whose host application hands it buffers but no
+ * allocator, or a loop that must not call cudaMalloc/cudaFree (they can
+ * synchronise the whole device) -- the scratch is a
  * fixed 16 MiB device array inside the library (held by every GPU that loads
  * the library until the process exits), so the call takes no workspace and
  * calls no allocator.  Limit: 65,536 frames per call (any atom count); larger

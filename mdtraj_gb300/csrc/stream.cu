@@ -962,9 +962,11 @@ int gbrmsd_rotations(const float* x, int64_t n_frames, int32_t n_atoms, int32_t 
 }
 
 // For callers that cannot allocate device memory when they need RMSDs -- for
-// example code that runs while a CUDA graph is being captured, inside another
-// runtime's memory pool, or in a plugin that has no allocator of its own --
-// this variant of gbrmsd_rmsd_to_reference takes no workspace: its scratch is
+// example code running inside another runtime's memory pool (the pool owns
+// the device memory and must not see a cudaMalloc behind its back), a plugin
+// whose host application hands it buffers but no allocator, or a
+// latency-bound loop that must not call cudaMalloc/cudaFree (they can
+// synchronise the whole device) -- this variant of gbrmsd_rmsd_to_reference takes no workspace: its scratch is
 // g_noalloc_scratch above.  It calls no cudaMalloc/cudaFree.  The first call
 // on a device looks up the array's device address (cudaGetSymbolAddress) with
 // that device current; make that first call before any stream capture.  All

@@ -1,8 +1,10 @@
 """The allocation-free entry point gbrmsd_rmsd_to_reference_noalloc.
 
-Some callers cannot allocate device memory when they need RMSDs (code that
-runs during CUDA-graph capture, inside another runtime's memory pool, or a
-plugin without an allocator).  For them the library keeps a fixed 16 MiB
+Some callers cannot allocate device memory when they need RMSDs: code
+inside another runtime's memory pool (the pool owns the device memory), a
+plugin whose host application hands it buffers but no allocator, or a loop
+that must not call cudaMalloc/cudaFree (they can synchronise the device).
+For them the library keeps a fixed 16 MiB
 scratch array on the device and this entry point takes no workspace.  The
 test calls it through the C ABI, twice in a row (different shapes, then the
 same shape again, so state left by one call cannot leak into the next), and
