@@ -812,7 +812,9 @@ def run_reference(args) -> dict:
         "dtype": "f32",
         "data": "synthetic (seeded)",
         "config": {"workload": args.workload, "n_frames": F, "n_atoms": A, "layout": "atom-major (host)",
-                   "precentered": False, "note": "each step timed on a bounded frame sample"},
+                   "precentered": False, "sigma_nm": [s_lo, s_hi], "exact_copy_fraction": exact,
+                   "parallelism": "OpenMP over the host cores",
+                   "note": "each step timed on a bounded frame sample"},
         "cpu_baseline": base,
         "e2e": {"value": round(base["value"], 1), "unit": "frames/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
