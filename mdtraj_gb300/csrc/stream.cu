@@ -2,7 +2,7 @@
 //
 // Work per call (all on one stream, no host synchronisation):
 //   1. stream_kernel   one pass over the frames.  Persistent CTAs (one per
-//                      SM), 8 warps each; every warp owns a ring of
+//                      SM), 8 or 16 warps each (kCfgs); every warp owns a ring of
 //                      shared-memory stages fed by 1-D bulk async copies
 //                      (cp.async.bulk + mbarrier, issued by lane 0) and
 //                      walks a static round-robin list of (frame, split)
