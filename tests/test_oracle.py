@@ -132,3 +132,62 @@ def test_reference_c_xtc_reader_matches_fixture(golden):
         np.testing.assert_array_equal(step, g[f"{name}__step"])
         np.testing.assert_array_equal(time, g[f"{name}__time"])
         np.testing.assert_array_equal(box, g[f"{name}__box"])
+
+
+def _degenerate_case(shape, rng):
+    """(frames (F, A, 3), reference frame index) for structures where the QCP
+    quartic is badly conditioned or the sums are tiny."""
+    F = 48
+    if shape == "collinear":
+        base = np.outer(np.linspace(-2, 2, 40), [0.3, -0.5, 0.8])
+    elif shape == "planar":
+        base = np.concatenate([rng.uniform(-2, 2, (60, 2)), np.zeros((60, 1))], 1)
+    elif shape.startswith("atoms"):
+        base = rng.uniform(0, 3, (int(shape[5:]), 3))
+    else:  # "random"
+        base = rng.uniform(0, 4, (333, 3))
+    x = np.empty((F,) + base.shape, dtype=np.float32)
+    for f in range(F):
+        q = rng.normal(size=4)
+        q /= np.linalg.norm(q)
+        w, a, b, c = q
+        R = np.array([[1 - 2 * (b * b + c * c), 2 * (a * b - c * w), 2 * (a * c + b * w)],
+                      [2 * (a * b + c * w), 1 - 2 * (a * a + c * c), 2 * (b * c - a * w)],
+                      [2 * (a * c - b * w), 2 * (b * c + a * w), 1 - 2 * (a * a + b * b)]])
+        noise = rng.normal(scale=0.05 * (f % 4 != 0), size=base.shape)  # every 4th frame an exact copy
+        x[f] = (base + noise) @ R.T + rng.uniform(-2, 2, 3)
+    return x
+
+
+SHAPES = ["planar", "atoms1", "atoms3", "atoms4", "random", "collinear", "atoms2"]
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+def test_port_restates_the_reference_on_degenerate_structures(shape):
+    """The C restatement against the reference's own compiled kernels on
+    planar, collinear and few-atom structures, with exact rotated copies
+    among the frames (where both cancel: the float32 QCP returns ~1e-3 nm
+    instead of 0).  Where the quartic's largest root is simple the two agree
+    to 2e-5 nm and both meet the parity bar of the FP64 oracle.  Collinear
+    and 2-atom structures give a double root, where the closed-form float32
+    solve is ill-conditioned: there the reference itself is off the FP64
+    oracle by 1e-3 to 3e-2 nm (6e-3 nm on these cases), and the port
+    reproduces that error envelope, not the reference's bits."""
+    try:
+        port, ref = cpu.CpuRmsd("port"), cpu.CpuRmsd("reference")
+    except (FileNotFoundError, OSError):
+        pytest.skip("reference CPU library not buildable here")
+    rng = np.random.default_rng(1000 + SHAPES.index(shape))
+    x = _degenerate_case(shape, rng)
+    want = fp64.kabsch_rmsd(x.astype(np.float64), x[0].astype(np.float64))
+    a = port.md_rmsd(x.copy(), x[0].copy())
+    b = ref.md_rmsd(x.copy(), x[0].copy())
+    assert np.all(np.isfinite(a)) and np.all(np.isfinite(b))
+    copies = np.arange(len(x)) % 4 == 0
+    assert np.abs(a[copies] - want[copies]).max() <= 5e-3 and np.abs(b[copies] - want[copies]).max() <= 5e-3
+    ea, eb = np.abs(a - want)[~copies], np.abs(b - want)[~copies]
+    if shape in ("collinear", "atoms2"):
+        assert ea.max() <= 2 * eb.max() + 1e-5, (shape, ea.max(), eb.max())
+    else:
+        np.testing.assert_allclose(a[~copies], b[~copies], atol=2e-5, err_msg=shape)
+        assert ea.max() <= ABS_TOL and eb.max() <= ABS_TOL, (shape, ea.max(), eb.max())
