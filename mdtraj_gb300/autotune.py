@@ -13,6 +13,7 @@ from __future__ import annotations
 import json
 import math
 import os
+import tempfile
 from pathlib import Path
 
 import numpy as np
@@ -48,11 +49,22 @@ def load_cache() -> dict:
 
 
 def save_cache(cache: dict) -> None:
+    """Writes the cache atomically: a private temporary file in the same
+    directory, then a rename, so processes or threads tuning at the same time
+    never see (or leave) a partly written file; the last writer wins."""
     p = cache_path()
     p.parent.mkdir(parents=True, exist_ok=True)
-    tmp = p.with_suffix(".tmp")
-    tmp.write_text(json.dumps(cache, indent=1, sort_keys=True))
-    os.replace(tmp, p)
+    fd, tmp = tempfile.mkstemp(prefix=p.name + ".", suffix=".tmp", dir=p.parent)
+    try:
+        with os.fdopen(fd, "w") as f:
+            f.write(json.dumps(cache, indent=1, sort_keys=True))
+        os.replace(tmp, p)
+    except BaseException:
+        try:
+            os.unlink(tmp)
+        except OSError:
+            pass
+        raise
 
 
 def tune_ragged(batch, reps: int = 3) -> dict:

@@ -139,6 +139,35 @@ def test_autotune_bucket_and_cache_roundtrip(tmp_path, monkeypatch):
     assert autotune.load_cache()[b1]["config"] == 2
 
 
+def test_autotune_cache_writers_do_not_collide(tmp_path, monkeypatch):
+    """Eight threads saving different caches at once: every save succeeds,
+    the file always parses as one complete cache, and no temporary file is
+    left behind."""
+    import threading
+
+    from mdtraj_gb300 import autotune
+
+    monkeypatch.setenv("MDTRAJ_GB300_CACHE", str(tmp_path))
+    errors = []
+
+    def writer(k):
+        try:
+            for i in range(50):
+                autotune.save_cache({f"ragged:{k}": {"config": i, "pad": "x" * 4096}})
+                got = autotune.load_cache()
+                assert len(got) == 1 and next(iter(got.values()))["pad"] == "x" * 4096
+        except BaseException as e:  # re-raised on the main thread
+            errors.append(e)
+
+    threads = [threading.Thread(target=writer, args=(k,)) for k in range(8)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors[:1]
+    assert [p.name for p in tmp_path.iterdir()] == ["autotune.json"]
+
+
 def test_ragged_layout_is_padded_and_aligned():
     from mdtraj_gb300 import RaggedBatch
 
