@@ -85,6 +85,10 @@ __host__ __device__ __forceinline__ double qcp_lambda_max(const double* m, doubl
     const double p = a * lam + c0;            // P(lam)
     const double dp = 2.0 * l2 * lam + b + a; // P'(lam)
     if (!(dp != 0.0)) break;
+    // P(lam) at its rounding floor: lam is a root to working precision (at
+    // a double root, as for collinear structures, P' is rounding noise too
+    // and a step would be noise over noise)
+    if (fabs(p) <= 32.0 * 2.220446049250313e-16 * (l2 * l2 + fabs(c2) * l2 + fabs(c1 * lam) + fabs(c0))) break;
     const double step = p / dp;
     lam -= step;
     if (!(fabs(step) > 1e-15 * fabs(lam))) {
@@ -140,6 +144,9 @@ __host__ __device__ __forceinline__ double qcp_lambda_max_mixed(const double* m,
     const float pv = a * x + a0;
     const float dp = 2.0f * x2 * x + b + a;
     if (!(dp != 0.0f)) break;
+    // at the rounding floor of P: x is a root to FP32 precision (see the
+    // FP64 loop below); starting from the upper bound, it is the largest
+    if (fabsf(pv) <= 32.0f * 1.1920929e-7f * (x2 * x2 + fabsf(a2) * x2 + fabsf(a1 * x) + fabsf(a0))) break;
 #ifdef __CUDA_ARCH__
     const float step = __fdividef(pv, dp);
 #else
@@ -157,6 +164,10 @@ __host__ __device__ __forceinline__ double qcp_lambda_max_mixed(const double* m,
     const double pv = a * lam + c0;
     const double dp = 2.0 * l2 * lam + b + a;
     if (!(dp != 0.0)) break;
+    // P(lam) at its rounding floor: lam is a root to working precision (at
+    // a double root, as for collinear structures, P' is rounding noise too
+    // and a step would be noise over noise)
+    if (fabs(pv) <= 32.0 * 2.220446049250313e-16 * (l2 * l2 + fabs(c2) * l2 + fabs(c1 * lam) + fabs(c0))) break;
     const float dpf = (float)fabs(dp);
     const double step = (dpf > 1e-30f && dpf < 1e30f) ? pv * (double)(1.0f / (float)dp) : pv / dp;
     lam -= step;
@@ -176,9 +187,9 @@ __host__ __device__ __forceinline__ double qcp_lambda_max_mixed(const double* m,
 // |v_i|).  The adjugate entries come from the twelve 2x2 minors of rows
 // {0,1} and {2,3} (Laplace expansion), ~70 FP64 operations instead of the 16
 // 3x3 cofactors (~220).  Returns false when B has no well-defined null vector
-// (all four diagonal cofactors vanish), in which case R is the identity.
-__host__ __device__ __forceinline__ bool qcp_rotation(const double* m, double lam, double* rot) {
-  const Key4 k = key_matrix(m);
+// (all four diagonal cofactors vanish even after the shift below), in which
+// case R is the identity.
+__host__ __device__ __forceinline__ double qcp_adj_row(const Key4& k, double lam, double (&q)[4]) {
   const double b00 = k.k00 - lam, b11 = k.k11 - lam, b22 = k.k22 - lam, b33 = k.k33 - lam;
   const double b01 = k.k01, b02 = k.k02, b03 = k.k03, b12 = k.k12, b13 = k.k13, b23 = k.k23;
   const double u0 = b00 * b11 - b01 * b01, u1 = b00 * b12 - b01 * b02, u2 = b00 * b13 - b01 * b03;
@@ -189,7 +200,6 @@ __host__ __device__ __forceinline__ bool qcp_rotation(const double* m, double la
   const double a11 = b00 * w5 - b02 * w2 + b03 * w1;
   const double a22 = b03 * u4 - b13 * u2 + b33 * u0;
   const double a33 = b02 * u3 - b12 * u1 + b22 * u0;
-  double q[4];
   double best = fabs(a00);
   q[0] = a00;
   q[1] = -b01 * w5 + b02 * w4 - b03 * w3;
@@ -215,6 +225,24 @@ __host__ __device__ __forceinline__ bool qcp_rotation(const double* m, double la
     q[2] = -b03 * u3 + b13 * u1 - b23 * u0;
     q[3] = a33;
   }
+  return best;
+}
+
+__host__ __device__ __forceinline__ bool qcp_rotation(const double* m, double lam, double* rot) {
+  const Key4 k = key_matrix(m);
+  double q[4];
+  const double best = qcp_adj_row(k, lam, q);
+  // When the largest eigenvalue of K is double (collinear structures, every
+  // 2-atom selection) and lam sits on it to rounding (exact copies: lam is
+  // the upper bound (G_a + G_b) / 2 itself), every cofactor of K - lam I is
+  // rounding noise and so would be the rotation.  Shifted by
+  // eps = 1e-9 * |K|, the adjugate is eps * c * (v1 v1^T + v2 v2^T) + O(eps^2)
+  // with v1, v2 spanning the eigenspace, so its rows give an optimal
+  // rotation; where the two top eigenvalues differ by g < 1e-12 |K| the
+  // shift changes the residual by at most ~2 g / n_atoms.  Other cases keep
+  // the unshifted row.
+  const double sk = fabs(lam) + fabs(k.k00) + fabs(k.k11) + fabs(k.k22) + fabs(k.k33);
+  if (sk > 0.0 && best < 1e-12 * sk * sk * sk) qcp_adj_row(k, lam + 1e-9 * sk, q);
   const double n = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
   if (!(n > 0.0) || !(n < 1e300)) {
     rot[0] = rot[4] = rot[8] = 1.0;
