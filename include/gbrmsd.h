@@ -110,17 +110,29 @@ int gbrmsd_rmsd_to_reference(const float* x, int64_t n_frames, int32_t n_atoms, 
  * synchronise the whole device) -- the scratch is a
  * fixed 16 MiB device array inside the library (held by every GPU that loads
  * the library until the process exits), so the call takes no workspace and
- * calls no allocator.  Limit: 65,536 frames per call (any atom count); larger
- * requests fail with GBRMSD_E_WORKSPACE before any work is queued.  The first
- * call on a device resolves the array's address with that device current and
- * should come before any stream capture.  Calls share the array: work of two
- * calls that overlaps on the GPU races, so serialise them.  Arguments as for
- * gbrmsd_rmsd_to_reference. */
+ * calls no allocator.  Limit: gbrmsd_noalloc_max_frames(n_atoms) frames per
+ * call (about 68,700 on a 152-SM GB300, for any atom count); larger requests
+ * fail with GBRMSD_E_WORKSPACE before any work is queued.  The first call on a
+ * device resolves the array's address with that device current and should
+ * come before any stream capture; the address is kept for the life of the
+ * process, so the entry point must not be used after a cudaDeviceReset.
+ * Calls share the array: work of two calls that overlaps on the GPU races, so
+ * serialise them.  Arguments as for gbrmsd_rmsd_to_reference. */
 int gbrmsd_rmsd_to_reference_noalloc(const float* x, int64_t n_frames, int32_t n_atoms, int32_t n_padded,
                                      int64_t frame_stride, int32_t layout, int32_t mode,
                                      const void* ref_ws, const float* g_target, float g_ref,
                                      int64_t self_index, float* out_rmsd, float* out_centroid,
                                      float* out_trace, void* stream);
+
+/* Error word of the last gbrmsd_rmsd_to_reference_noalloc on the current
+ * device (it lives in the library's static scratch, which such callers cannot
+ * reach through a workspace pointer): synchronises `stream`, writes the word
+ * to *word when word is not NULL (bit 1 = a bounded wait expired, bit 2 =
+ * non-finite input) and returns GBRMSD_E_DEVICE when it is non-zero.  No
+ * reference counterpart.  gbrmsd_noalloc_max_frames: the largest frame count
+ * one call accepts for frames of n_atoms atoms on the current device. */
+int gbrmsd_noalloc_status(int32_t* word, void* stream);
+int64_t gbrmsd_noalloc_max_frames(int32_t n_atoms);
 
 /* ---- All-pairs RMSD matrix --------------------------------------------------
  * Replaces the clustering loop over md.rmsd(traj, traj, i, precentered=True)
@@ -295,8 +307,31 @@ int gbrmsd_center_inplace(float* x, int64_t n_frames, int32_t n_atoms, int32_t n
 
 /* Synchronises `stream` and returns GBRMSD_E_DEVICE if a kernel that used
  * this workspace recorded a device-side error (e.g. a bounded wait expired),
- * GBRMSD_OK otherwise.  The error word is cleared by the next call. */
+ * GBRMSD_OK otherwise.  The error word is cleared by the next call.
+ * gbrmsd_workspace_error_word writes the word itself: bit 1 (value 1) = a
+ * bounded wait expired (the results of that call are not valid); bit 2
+ * (value 2) = some frame had non-finite coordinates (its RMSD is 0, as the
+ * reference's clamp of a NaN msd gives, src/theobald_rmsd.cpp:275-277). */
 int gbrmsd_workspace_status(const void* ws, void* stream);
+int gbrmsd_workspace_error_word(const void* ws, int32_t* word, void* stream);
+
+/* ---- Failure detection ------------------------------------------------------
+ * Every wait of the streaming kernels on a bulk copy is bounded in wall time
+ * (the GPU's global timer); when a wait runs out the kernel records bit 1 in
+ * the error word, waits (bounded) for its copies still in flight and returns,
+ * so the context stays usable and the caller sees GBRMSD_E_DEVICE from the
+ * status calls.  The reference has no counterpart (its CPU loops cannot
+ * stall; its only failure report is a printed warning, theobald_rmsd.cpp:
+ * 195-215).  Process-wide settings: do not change them while other calls run.
+ *   gbrmsd_set_wait_limit_ns  limit of each bounded wait (0 = default 2 s;
+ *                             1 us .. 60 s); read at each launch.
+ *   gbrmsd_test_skip_copy     test hook: the streaming kernel of later
+ *                             gbrmsd_rmsd_to_reference calls never issues the
+ *                             first copy of work unit `unit` (-1 = off), so a
+ *                             wait runs out with nothing in flight.  Accepted
+ *                             only while the wait limit is <= 100 ms. */
+int gbrmsd_set_wait_limit_ns(uint64_t ns);
+int gbrmsd_test_skip_copy(int64_t unit);
 
 /* Launch configurations of the streaming kernel (warps per CTA, quads per
  * stage, stages per warp, reference in shared memory, reserved = 0).  By default the first configuration whose shared

@@ -3,6 +3,7 @@ libgbrmsd does the work.  Nothing here computes RMSDs."""
 from __future__ import annotations
 
 import os
+import warnings
 
 import numpy as np
 import torch
@@ -156,20 +157,39 @@ class DeviceReference:
         return float(np.float32(g.value)), cen
 
 
+def error_word(ws: torch.Tensor) -> torch.Tensor:
+    """The device error word of a workspace (first int32 of its header) as a
+    one-element device tensor view."""
+    return ws[:4].view(torch.int32)
+
+
+def raise_on_error_word(word: int, what: str) -> None:
+    """Host side of the device error word (gbrmsd_workspace_error_word): an
+    expired bounded wait raises; non-finite coordinates warn (their RMSD is
+    0, the value the reference's clamp of a NaN msd returns)."""
+    if word & _lib.ERR_TIMEOUT:
+        raise _lib.GbrmsdError(_lib.E_DEVICE, f"{what}: a bounded wait on the GPU expired; the results are not valid")
+    if word & _lib.ERR_NONFINITE:
+        warnings.warn(f"{what}: some frames have non-finite coordinates; their RMSD is reported as 0, as "
+                      "mdtraj's clamp of a NaN msd gives", RuntimeWarning, stacklevel=3)
+
+
 def rmsd_to_reference(x: torch.Tensor, n_frames: int, n_atoms: int, n_padded: int, layout: int,
                       mode: int, ref: DeviceReference, *, g_target: torch.Tensor | None = None,
                       g_ref: float = 0.0, self_index: int = -1, out: torch.Tensor | None = None,
                       centroid_out: torch.Tensor | None = None,
-                      trace_out: torch.Tensor | None = None) -> torch.Tensor:
+                      trace_out: torch.Tensor | None = None, ws: torch.Tensor | None = None) -> torch.Tensor:
     """Device-resident RMSD of every frame of `x` to `ref` (see
     gbrmsd_rmsd_to_reference) on torch's current stream, which also orders
-    the workspace's reuse.  Returns the float32 rmsd tensor."""
+    the workspace's reuse.  Returns the float32 rmsd tensor.  Pass `ws`
+    (gbrmsd_rmsd_workspace_bytes) to read its error word afterwards."""
     stream = stream_handle()
     device = x.device
     if out is None:
         out = torch.empty(n_frames, dtype=torch.float32, device=device)
     nbytes = lib.gbrmsd_rmsd_workspace_bytes(n_frames, n_atoms)
-    ws = empty_bytes(nbytes, device)
+    if ws is None or ws.numel() < nbytes:
+        ws = empty_bytes(nbytes, device)
     frame_stride = 3 * n_padded
     check(lib.gbrmsd_rmsd_to_reference(
         ptr(x), n_frames, n_atoms, n_padded, frame_stride, layout, mode, ref.ws.data_ptr(),
@@ -284,6 +304,8 @@ def rmsd_host_frames(x: np.ndarray, ref: "DeviceReference", mode: int, *, g_targ
         if g_target is not None else None
     bufs = [torch.empty((C, 3 * Ap), dtype=torch.float32, device=device) for _ in range(min(ring, n_chunks))]
     ws = empty_bytes(lib.gbrmsd_rmsd_workspace_bytes(C, A), device)
+    # each chunk's call clears the workspace's error word: keep a copy per chunk
+    words = torch.zeros(n_chunks, dtype=torch.int32, device=device)
     host_ok = pageable_access()
     in_done = [torch.cuda.Event() for _ in range(n_chunks)]
     rmsd_done = [torch.cuda.Event() for _ in range(n_chunks)]
@@ -321,6 +343,7 @@ def rmsd_host_frames(x: np.ndarray, ref: "DeviceReference", mode: int, *, g_targ
                     ptr(g_dev[f0:f0 + n]) if g_dev is not None else None, float(g_ref), si,
                     out[f0:f0 + n].data_ptr(), cent[f0:f0 + n].data_ptr() if cent is not None else None, None,
                     ws.data_ptr(), ws.numel(), s_work.cuda_stream))
+                words[k:k + 1].copy_(error_word(ws))
                 rmsd_done[k].record(s_work)
                 if write_centred:
                     dst = x.ctypes.data + f0 * 12 * A
@@ -339,10 +362,13 @@ def rmsd_host_frames(x: np.ndarray, ref: "DeviceReference", mode: int, *, g_targ
         raise
     result = np.empty(F, dtype=np.float32)
     copy_rows(result.ctypes.data, 4 * F, out.data_ptr(), 4 * F, 4 * F, 1, 2, s_work.cuda_stream)
+    word = np.zeros(n_chunks, dtype=np.int32)
+    copy_rows(word.ctypes.data, word.nbytes, words.data_ptr(), word.nbytes, word.nbytes, 1, 2, s_work.cuda_stream)
     s_work.synchronize()
     s_in.synchronize()
     if locks is not None:
         locks.release()
+    raise_on_error_word(int(np.bitwise_or.reduce(word)), "rmsd")
     if write_centred and not host_ok:
         cent_h = np.empty((F, 3), dtype=np.float32)
         copy_rows(cent_h.ctypes.data, cent_h.nbytes, cent.data_ptr(), cent_h.nbytes, cent_h.nbytes, 1, 2,
@@ -350,5 +376,5 @@ def rmsd_host_frames(x: np.ndarray, ref: "DeviceReference", mode: int, *, g_targ
         s_work.synchronize()
         check(lib.gbrmsd_host_subtract_centroids(x.ctypes.data, F, A, 3 * A, cent_h.ctypes.data, 0))
     # keep the device buffers alive until both streams are done
-    del bufs, ws, out, cent, g_dev
+    del bufs, ws, out, cent, g_dev, words
     return result

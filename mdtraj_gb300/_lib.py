@@ -25,6 +25,10 @@ MODE_CENTER = 0
 MODE_PRECENTERED = 1
 MODE_NOSUPERPOSE = 2
 
+# device error word bits (gbrmsd_workspace_error_word)
+ERR_TIMEOUT = 1
+ERR_NONFINITE = 2
+
 _vp = C.c_void_p
 _i32 = C.c_int32
 _i64 = C.c_int64
@@ -71,6 +75,11 @@ SIGNATURES: dict[str, tuple] = {
     "gbrmsd_ragged_rmsd": (C.c_int, [_vp, _vp, _vp, _vp, _sz, _vp]),
     "gbrmsd_center_inplace": (C.c_int, [_vp, _i64, _i32, _i32, _i64, _i32, _vp, _vp, _vp, _sz, _vp]),
     "gbrmsd_workspace_status": (C.c_int, [_vp, _vp]),
+    "gbrmsd_workspace_error_word": (C.c_int, [_vp, _vp, _vp]),
+    "gbrmsd_noalloc_status": (C.c_int, [_vp, _vp]),
+    "gbrmsd_noalloc_max_frames": (_i64, [_i32]),
+    "gbrmsd_set_wait_limit_ns": (C.c_int, [C.c_uint64]),
+    "gbrmsd_test_skip_copy": (C.c_int, [_i64]),
     "gbrmsd_stream_config_count": (C.c_int, []),
     "gbrmsd_stream_config_select": (C.c_int, [_i32]),
     "gbrmsd_stream_config_describe": (C.c_int, [_i32, _i32, _vp]),

@@ -218,9 +218,14 @@ def _multiple(xyz1, xyz2, g1, g2, frame, layout):
     g_dev = torch.from_numpy(np.ascontiguousarray(g2[:n_frames])).to(device)
     self_index = _alias_index(xyz2, ref_frame)
     out = torch.empty(n_frames, dtype=torch.float32, device=device)
+    ws = D.empty_bytes(lib.gbrmsd_rmsd_workspace_bytes(n_frames, n_atoms), device)
     D.rmsd_to_reference(x_dev, n_frames, n_atoms, n_padded, layout, _lib.MODE_PRECENTERED, ref,
-                        g_target=g_dev, g_ref=float(g1[frame]), self_index=self_index, out=out)
-    return D.to_host(out, stream)
+                        g_target=g_dev, g_ref=float(g1[frame]), self_index=self_index, out=out, ws=ws)
+    result = D.to_host(out, stream)
+    word = _lib.C.c_int32(0)
+    check(lib.gbrmsd_workspace_error_word(ws.data_ptr(), _lib.C.addressof(word), stream))
+    D.raise_on_error_word(word.value, "getMultipleRMSDs")
+    return result
 
 
 def getMultipleRMSDs_axis_major(xyz1, xyz2, g1, g2, frame, parallel=True):

@@ -55,5 +55,10 @@ def allpairs_rmsd(target, precentered: bool = False, method: str = "tensor") -> 
     device = D.require_device()
     stream = D.stream_handle()
     x_dev, n_padded = D.frames_to_device(xyz, _lib.ATOM_MAJOR, device, stream)
-    out = allpairs_device(x_dev, F, A, n_padded, _lib.ATOM_MAJOR, centre=not precentered, method=method)
-    return D.to_host(out, stream)
+    ws = D.empty_bytes(lib.gbrmsd_allpairs_workspace_bytes(F, A), device)
+    out = allpairs_device(x_dev, F, A, n_padded, _lib.ATOM_MAJOR, centre=not precentered, method=method, ws=ws)
+    result = D.to_host(out, stream)
+    # raises when the device recorded an error (an expired wait, a full
+    # refinement list)
+    check(lib.gbrmsd_allpairs_status(ws.data_ptr(), None, stream))
+    return result

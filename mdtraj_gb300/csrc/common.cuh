@@ -171,6 +171,31 @@ GB_DEV bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* err, uint32_t
   return false;
 }
 
+// Nanoseconds of the GPU's global timer.
+GB_DEV uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Wait bounded in wall time: false (and DEV_ERR_TIMEOUT in *err) when the
+// phase has not completed `limit_ns` nanoseconds after the first failed
+// try_wait.  2^24 rounds of 64 try_waits stay as a backstop should the
+// timer not advance.  The streaming kernels take the limit from their
+// launch arguments (gbrmsd_set_wait_limit_ns).
+GB_DEV bool mbar_wait_timed(uint64_t* bar, uint32_t parity, int* err, uint64_t limit_ns) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = global_ns();
+  for (uint32_t round = 0; round < (1u << 24); ++round) {
+#pragma unroll 1
+    for (int i = 0; i < 64; ++i)
+      if (mbar_try_wait(bar, parity)) return true;
+    if (global_ns() - t0 > limit_ns) break;
+  }
+  if (err) atomicOr(err, DEV_ERR_TIMEOUT);
+  return false;
+}
+
 GB_DEV float4 lds4(const float* p) { return *reinterpret_cast<const float4*>(p); }
 
 GB_DEV float4 ldg4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }

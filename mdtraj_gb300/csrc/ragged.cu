@@ -44,6 +44,7 @@ struct RaggedArgs {
   const unsigned char* ref_base;
   double* sums;
   int* err;
+  uint64_t wait_ns;  // limit of each bounded wait (gbrmsd_set_wait_limit_ns)
 };
 
 constexpr size_t REF_INFO_BYTES = 256;
@@ -288,7 +289,7 @@ __global__ void __launch_bounds__(WARPS * 32, 1) ragged_stream_kernel(const Ragg
   float shift[3] = {0.f, 0.f, 0.f};
 
   while (consumed < issued) {
-    if (!mbar_wait_bounded(&bars[slot], (phases >> slot) & 1u, p.err)) {
+    if (!mbar_wait_timed(&bars[slot], (phases >> slot) & 1u, p.err, p.wait_ns)) {
       failed = true;
       break;
     }
@@ -368,11 +369,13 @@ __global__ void __launch_bounds__(WARPS * 32, 1) ragged_stream_kernel(const Ragg
     }
   }
   if (failed) {
-    while (consumed < issued) {
-      if (!mbar_wait_bounded(&bars[slot], (phases >> slot) & 1u, nullptr)) break;
+    // bounded wait on every outstanding stage (the one that timed out
+    // included) so that no copy is in flight into shared memory at exit
+    const int outstanding = issued - consumed;
+    for (int i = 0; i < outstanding; ++i) {
+      mbar_wait_timed(&bars[slot], (phases >> slot) & 1u, nullptr, p.wait_ns);
       phases ^= 1u << slot;
       slot = (slot + 1 == NSTAGE) ? 0 : slot + 1;
-      ++consumed;
     }
   }
 }
@@ -667,6 +670,7 @@ int gbrmsd_ragged_rmsd(const float* x, float* out, const gbrmsd_ragged_plan_t* p
   a.ref_base = b + ref_off;
   a.sums = reinterpret_cast<double*>(b + sums_off);
   a.err = &hdr->err;
+  a.wait_ns = wait_limit_ns();
   prof_begin(st);
   int rc = launch_ragged(plan->config, a, plan->grid, st);
   if (rc) return rc;

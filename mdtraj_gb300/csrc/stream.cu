@@ -96,6 +96,9 @@ __device__ __forceinline__ bool cursor_next(Cursor& cur, int64_t W, int32_t S, i
 template <int LAYOUT, int CQ>
 __device__ __forceinline__ void issue_chunk(const StreamArgs& p, const void* tmap, const Cursor& cur,
                                             unsigned char* stage, uint64_t* bar) {
+  // failure-detection test hook: this chunk is never issued, so the wait on
+  // its stage runs out (nothing is put in flight for it)
+  if (cur.c == 0 && cur.unit == p.skip_unit) return;
   const int32_t qb = cur.q0 + cur.c * CQ;
   const int32_t nq = min(CQ, cur.q1 - qb);
   if (LAYOUT == ATOM_MAJOR) {
@@ -188,7 +191,7 @@ __global__ void __launch_bounds__(WARPS * 32, 1) stream_kernel(const StreamArgs 
     }
     const int32_t qb = cc.q0 + cc.c * CQ;
     const int32_t nq = min(CQ, cc.q1 - qb);
-    if (!mbar_wait_bounded(&bars[slot], (phases >> slot) & 1u, p.err)) {
+    if (!mbar_wait_timed(&bars[slot], (phases >> slot) & 1u, p.err, p.wait_ns)) {
       failed = true;
       break;
     }
@@ -318,12 +321,15 @@ __global__ void __launch_bounds__(WARPS * 32, 1) stream_kernel(const StreamArgs 
   }
 
   if (failed) {
-    // Drain this warp's copies still in flight (bounded), then leave.
-    while (consumed < issued) {
-      if (!mbar_wait_bounded(&bars[slot], (phases >> slot) & 1u, nullptr)) break;
+    // Wait (bounded) on every stage this warp still has outstanding, the one
+    // that timed out included, so that no copy is left in flight into shared
+    // memory when the CTA exits; a stage whose copy never arrives costs one
+    // more bounded wait and does not stop the others from being drained.
+    const int64_t outstanding = issued - consumed;
+    for (int64_t i = 0; i < outstanding; ++i) {
+      mbar_wait_timed(&bars[slot], (phases >> slot) & 1u, nullptr, p.wait_ns);
       phases ^= 1u << slot;
       slot = (slot + 1 == NSTAGE) ? 0 : slot + 1;
-      ++consumed;
     }
   }
 }
@@ -379,6 +385,7 @@ struct RefineArgs {
   const RefineEntry* list;
   const int* count;
   float* out_rmsd;
+  float* out_centroid;  // entries with seg = -1: centroid of a non-finite frame
 };
 
 template <int LAYOUT>
@@ -392,6 +399,24 @@ __global__ void __launch_bounds__(256) refine_kernel(const RefineArgs r) {
   for (int64_t e = gw; e < n; e += W) {
     const RefineEntry en = r.list[e];
     const float* fr = r.x + en.frame * r.frame_stride;
+    if (en.seg < 0) {
+      // centroid of a frame with non-finite coordinates as the reference
+      // computes it (src/center_generic.h: double sum, divide, round to
+      // float), which keeps +-inf where the shifted sums give NaN
+      double s[3] = {0.0, 0.0, 0.0};
+      for (int32_t q = lane; q < Q; q += 32) {
+        float ax[4], ay[4], az[4];
+        load_frame_quad<LAYOUT>(fr, Ap, q, ax, ay, az);
+        const int nv = A - 4 * q;
+#pragma unroll
+        for (int t = 0; t < 4; ++t)
+          if (t < nv) { s[0] += ax[t]; s[1] += ay[t]; s[2] += az[t]; }
+      }
+      for (int k = 0; k < 3; ++k) s[k] = warp_sum_d(s[k]);
+      if (lane == 0 && r.out_centroid)
+        for (int k = 0; k < 3; ++k) r.out_centroid[3 * en.frame + k] = (float)(s[k] / (double)A);
+      continue;
+    }
     CF acc = cf_zero();
     int32_t q = lane;
     for (; q + 32 * (U - 1) < Q; q += 32 * U) {
@@ -434,7 +459,7 @@ __global__ void __launch_bounds__(256) refine_kernel(const RefineArgs r) {
 
 template <int LAYOUT>
 __global__ void __launch_bounds__(256) center_writeback_kernel(float* x, int64_t F, int32_t A, int32_t Ap,
-                                                               int64_t frame_stride, const float* centroid,
+                                                               int64_t frame_stride, float* centroid,
                                                                float* traces) {
   const int lane = threadIdx.x & 31;
   const int64_t W = (int64_t)gridDim.x * (blockDim.x >> 5);
@@ -442,7 +467,31 @@ __global__ void __launch_bounds__(256) center_writeback_kernel(float* x, int64_t
   const int32_t Q = (A + 3) >> 2;
   for (int64_t f = gw; f < F; f += W) {
     float* fr = x + f * frame_stride;
-    const float mx = centroid[3 * f], my = centroid[3 * f + 1], mz = centroid[3 * f + 2];
+    float mx = centroid[3 * f], my = centroid[3 * f + 1], mz = centroid[3 * f + 2];
+    if (!(isfinite(mx) && isfinite(my) && isfinite(mz))) {
+      // non-finite coordinates: the shifted one-pass sums give NaN where the
+      // reference's double sum gives +-inf (src/center_generic.h), so this
+      // frame's centroid is recomputed the reference's way first
+      double s[3] = {0.0, 0.0, 0.0};
+      for (int32_t q = lane; q < Q; q += 32) {
+        float ax[4], ay[4], az[4];
+        load_frame_quad<LAYOUT>(fr, Ap, q, ax, ay, az);
+        const int nv = A - 4 * q;
+#pragma unroll
+        for (int t = 0; t < 4; ++t)
+          if (t < nv) { s[0] += ax[t]; s[1] += ay[t]; s[2] += az[t]; }
+      }
+      for (int k = 0; k < 3; ++k) s[k] = warp_sum_d(s[k]);
+      mx = (float)(s[0] / (double)A);
+      my = (float)(s[1] / (double)A);
+      mz = (float)(s[2] / (double)A);
+      __syncwarp();
+      if (lane == 0) {
+        centroid[3 * f] = mx;
+        centroid[3 * f + 1] = my;
+        centroid[3 * f + 2] = mz;
+      }
+    }
     CF acc = cf_zero();
     for (int32_t q = lane; q < Q; q += 32) {
       const int nv = A - 4 * q;
@@ -644,7 +693,10 @@ int encode_axis_map(CUtensorMap* tm, const StreamArgs& a) {
   return GBRMSD_OK;
 }
 
-int launch_stream(int layout, int mode, const StreamArgs& a, const StreamCfg& c, cudaStream_t st) {
+int launch_stream(int layout, int mode, const StreamArgs& args, const StreamCfg& c, cudaStream_t st) {
+  StreamArgs a = args;
+  a.wait_ns = wait_limit_ns();
+  a.skip_unit = skip_unit_hook();
   const bool use_ref = mode != MODE_TRACE;
   const size_t smem = stream_smem_bytes(c, a.n_padded, use_ref);
   const int grid = sm_count();
@@ -722,6 +774,16 @@ int g_prof_n = 0;
 cudaEvent_t g_ev[kProfMax][2];
 }  // namespace
 
+// Failure-detection settings (gbrmsd_set_wait_limit_ns, gbrmsd_test_skip_copy).
+namespace {
+constexpr uint64_t kDefaultWaitNs = 2000000000ull;  // 2 s per bounded wait
+std::atomic<uint64_t> g_wait_ns{kDefaultWaitNs};
+std::atomic<int64_t> g_skip_unit{-1};
+}  // namespace
+
+uint64_t wait_limit_ns() { return g_wait_ns.load(std::memory_order_relaxed); }
+int64_t skip_unit_hook() { return g_skip_unit.load(std::memory_order_relaxed); }
+
 void prof_begin(cudaStream_t st) {
   if (g_prof_n < g_prof_cap) cudaEventRecord(g_ev[g_prof_n][0], st);
 }
@@ -737,13 +799,33 @@ void prof_end(cudaStream_t st) {
 
 // Scratch of gbrmsd_rmsd_to_reference_noalloc: a fixed device array that
 // exists on every GPU that loads this library, for the life of the process.
-// 16 MiB covers the partial-sum records, refinement list and centroids of up
-// to 65,536 frames of any atom count on a 152-SM GB300.
+// 16 MiB covers the partial-sum records, refinement list and centroids of
+// gbrmsd_noalloc_max_frames(n_atoms) frames: about 68,700 of any atom count on
+// a 152-SM GB300 (244 bytes per frame).
 constexpr size_t kNoallocScratchBytes = 16u << 20;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
 static std::atomic<void*> g_noalloc_scratch_addr[64] = {};
 
 using namespace gb;
+
+// Device address of g_noalloc_scratch on the current device.  In host code
+// the array's name stands for a host-side shadow, not for device memory, so
+// the address is looked up once per device, with that device current, and
+// kept for the life of the process (a cudaDeviceReset destroys the context
+// it belongs to: the entry point must not be used after one).
+static int noalloc_scratch(void** out) {
+  int dev = 0;
+  GB_CUDA_TRY(cudaGetDevice(&dev), "cudaGetDevice");
+  if (dev < 0 || dev >= 64) return set_error(GBRMSD_E_UNSUPPORTED, "rmsd_to_reference_noalloc: device %d", dev);
+  void* scratch = g_noalloc_scratch_addr[dev].load(std::memory_order_acquire);
+  if (!scratch) {
+    GB_CUDA_TRY(cudaGetSymbolAddress(&scratch, g_noalloc_scratch), "cudaGetSymbolAddress(g_noalloc_scratch)");
+    if (!scratch) return set_error(GBRMSD_E_CUDA, "rmsd_to_reference_noalloc: null scratch address");
+    g_noalloc_scratch_addr[dev].store(scratch, std::memory_order_release);
+  }
+  *out = scratch;
+  return GBRMSD_OK;
+}
 
 extern "C" {
 
@@ -874,6 +956,7 @@ int gbrmsd_rmsd_to_reference(const float* x, int64_t n_frames, int32_t n_atoms, 
     ra.list = fa.refine;
     ra.count = fa.refine_count;
     ra.out_rmsd = out_rmsd;
+    ra.out_centroid = out_centroid;
     // one warp per queued frame; the queue is usually short or empty
     const int rgrid = sm_count() * 2;
     if (layout == ATOM_MAJOR)
@@ -952,6 +1035,7 @@ int gbrmsd_rotations(const float* x, int64_t n_frames, int32_t n_atoms, int32_t 
     ra.list = fa.refine;
     ra.count = fa.refine_count;
     ra.out_rmsd = out_rmsd;
+    ra.out_centroid = nullptr;
     if (layout == ATOM_MAJOR)
       refine_kernel<ATOM_MAJOR><<<sm_count() * 4, 256, 0, st>>>(ra);
     else
@@ -978,23 +1062,18 @@ int gbrmsd_rmsd_to_reference_noalloc(const float* x, int64_t n_frames, int32_t n
                                      const float* g_target, float g_ref, int64_t self_index, float* out_rmsd,
                                      float* out_centroid, float* out_trace, void* stream) {
   clear_error();
-  int dev = 0;
-  GB_CUDA_TRY(cudaGetDevice(&dev), "cudaGetDevice");
-  if (dev < 0 || dev >= 64) return set_error(GBRMSD_E_UNSUPPORTED, "rmsd_to_reference_noalloc: device %d", dev);
-  void* scratch = g_noalloc_scratch_addr[dev].load(std::memory_order_acquire);
-  if (!scratch) {
-    GB_CUDA_TRY(cudaGetSymbolAddress(&scratch, g_noalloc_scratch), "cudaGetSymbolAddress(g_noalloc_scratch)");
-    if (!scratch) return set_error(GBRMSD_E_CUDA, "rmsd_to_reference_noalloc: null scratch address");
-    g_noalloc_scratch_addr[dev].store(scratch, std::memory_order_release);
-  }
+  void* scratch = nullptr;
+  const int rc = noalloc_scratch(&scratch);
+  if (rc) return rc;
   if (n_frames < 0 || n_atoms < 0) return set_error(GBRMSD_E_INVALID, "negative n_frames/n_atoms");
   const size_t need = gbrmsd_rmsd_workspace_bytes(n_frames, n_atoms);
   if (need > kNoallocScratchBytes)
     return set_error(GBRMSD_E_WORKSPACE,
                      "rmsd_to_reference_noalloc: %lld frames of %d atoms need %zu bytes of scratch but the static "
-                     "scratch holds %zu (at most 65536 frames per call); split the call or use "
+                     "scratch holds %zu (at most %lld frames of %d atoms per call); split the call or use "
                      "gbrmsd_rmsd_to_reference with a workspace",
-                     (long long)n_frames, n_atoms, need, kNoallocScratchBytes);
+                     (long long)n_frames, n_atoms, need, kNoallocScratchBytes,
+                     (long long)gbrmsd_noalloc_max_frames(n_atoms), n_atoms);
   return gbrmsd_rmsd_to_reference(x, n_frames, n_atoms, n_padded, frame_stride, layout, mode, ref_ws, g_target,
                                   g_ref, self_index, out_rmsd, out_centroid, out_trace, scratch,
                                   kNoallocScratchBytes, stream);
@@ -1106,14 +1185,72 @@ int gbrmsd_profile_read(float* stream_kernel_ms, int32_t capacity) {
   return n;
 }
 
-int gbrmsd_workspace_status(const void* ws, void* stream) {
+int gbrmsd_workspace_error_word(const void* ws, int32_t* word, void* stream) {
   clear_error();
-  if (!ws) return set_error(GBRMSD_E_INVALID, "workspace_status: null workspace");
+  if (!ws || !word) return set_error(GBRMSD_E_INVALID, "workspace_error_word: null workspace or output");
   WsHeader h;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   GB_CUDA_TRY(cudaMemcpyAsync(&h, ws, sizeof(h), cudaMemcpyDeviceToHost, st), "copy header");
   GB_CUDA_TRY(cudaStreamSynchronize(st), "sync");
-  if (h.err) return set_error(GBRMSD_E_DEVICE, "device error word 0x%x (1 = bounded wait expired, 2 = non-finite input)", h.err);
+  *word = h.err;
+  return GBRMSD_OK;
+}
+
+int gbrmsd_workspace_status(const void* ws, void* stream) {
+  int32_t word = 0;
+  const int rc = gbrmsd_workspace_error_word(ws, &word, stream);
+  if (rc) return rc;
+  if (word)
+    return set_error(GBRMSD_E_DEVICE, "device error word 0x%x (1 = bounded wait expired, 2 = non-finite input)",
+                     word);
+  return GBRMSD_OK;
+}
+
+int gbrmsd_noalloc_status(int32_t* word, void* stream) {
+  clear_error();
+  void* scratch = nullptr;
+  const int rc = noalloc_scratch(&scratch);
+  if (rc) return rc;
+  int32_t w = 0;
+  const int rc2 = gbrmsd_workspace_error_word(scratch, &w, stream);
+  if (rc2) return rc2;
+  if (word) *word = w;
+  if (w)
+    return set_error(GBRMSD_E_DEVICE,
+                     "rmsd_to_reference_noalloc: device error word 0x%x (1 = bounded wait expired, 2 = non-finite "
+                     "input)", w);
+  return GBRMSD_OK;
+}
+
+int64_t gbrmsd_noalloc_max_frames(int32_t n_atoms) {
+  if (n_atoms < 0) return -1;
+  // the scratch a call needs grows with the frame count: largest F that fits
+  int64_t lo = 0, hi = (int64_t)kNoallocScratchBytes;  // a frame needs more than one byte
+  while (lo < hi) {
+    const int64_t mid = lo + (hi - lo + 1) / 2;
+    if (gbrmsd_rmsd_workspace_bytes(mid, n_atoms) <= kNoallocScratchBytes)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+int gbrmsd_set_wait_limit_ns(uint64_t ns) {
+  clear_error();
+  if (ns == 0) ns = kDefaultWaitNs;
+  if (ns < 1000ull || ns > 60000000000ull)
+    return set_error(GBRMSD_E_INVALID, "set_wait_limit_ns: limit must be 0 (default) or in [1 us, 60 s]");
+  g_wait_ns.store(ns, std::memory_order_relaxed);
+  return GBRMSD_OK;
+}
+
+int gbrmsd_test_skip_copy(int64_t unit) {
+  clear_error();
+  if (unit < -1) return set_error(GBRMSD_E_INVALID, "test_skip_copy: unit must be -1 (off) or >= 0");
+  if (unit >= 0 && wait_limit_ns() > 100000000ull)
+    return set_error(GBRMSD_E_INVALID, "test_skip_copy: set a wait limit of at most 100 ms first");
+  g_skip_unit.store(unit, std::memory_order_relaxed);
   return GBRMSD_OK;
 }
 

@@ -49,7 +49,14 @@ struct StreamArgs {
   int32_t splits;        // partial records per frame
   double* sums;          // [n_frames * splits][SUMS_STRIDE]
   int* err;
+  uint64_t wait_ns;      // limit of each bounded wait (gbrmsd_set_wait_limit_ns)
+  int64_t skip_unit;     // failure-detection test hook: the first chunk of this
+                         // unit is never issued (-1: off)
 };
+
+// Process-wide settings of the failure-detection hooks (stream.cu).
+uint64_t wait_limit_ns();
+int64_t skip_unit_hook();
 
 struct FinishArgs {
   int64_t n_frames;

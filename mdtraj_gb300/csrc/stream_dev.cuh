@@ -315,10 +315,25 @@ __device__ __forceinline__ void finish_frame(const FrameCtx& c, float* out_rmsd,
   bool finite = isfinite(ga) && isfinite(gb);
   for (int i = 0; i < 9; ++i) finite = finite && isfinite(m[i]);
   if (!finite) {
+    // Non-finite coordinates.  The reference's msd is then NaN and its clamp
+    // `if (rmsd2 > 0.0f)` returns 0 (src/theobald_rmsd.cpp:275-277), so the
+    // RMSD is 0 here too; the error word records that it happened.  Its
+    // rotation is NaN (qsqr < 1e-11f is false for NaN), as here.
     atomicOr(err, DEV_ERR_NONFINITE);
-    out_rmsd[f] = nanf("");
+    out_rmsd[f] = 0.f;
     if (c.out_rot)
       for (int i = 0; i < 9; ++i) c.out_rot[9 * f + i] = nanf("");
+    if (out_centroid && refine && c.mode == MODE_CENTER) {
+      // The shifted one-pass sums turn an infinite coordinate into NaN, where
+      // the reference's double sum gives +-inf: the refinement pass recomputes
+      // this frame's centroid by plain FP64 sums (marked by seg = -1).
+      RefineEntry e;
+      e.frame = c.refine_frame;
+      for (int i = 0; i < 9; ++i) e.rot[i] = 0.f;
+      for (int k = 0; k < 3; ++k) { e.mu_hi[k] = 0.f; e.mu_lo[k] = 0.f; }
+      e.seg = -1;
+      refine[atomicAdd(refine_count, 1)] = e;
+    }
     return;
   }
   int iters = 0;
