@@ -56,7 +56,30 @@ __device__ __forceinline__ float rn_dot4(float a0, float b0, float a1, float b1,
 
 // FP32 QCP on the quartic normalised by lam0 = (Ga + Gb) / 2 (root near 1).
 // Returns msd = 2 lam0 (1 - x) / n, x = normalised lambda_max.
-__device__ __forceinline__ float qcp_msd_f32(const float (&m)[9], float ga, float gb, float inv_n) {
+//
+// `unresolved` is set when the FP32 result cannot be trusted to 2e-5 nm.
+// That happens at (nearly) double roots: when one of the two structures is
+// (nearly) collinear, as every 2-atom selection is, M has rank ~1 and K's
+// top eigenvalue is doubled, and in FP32 the quartic fixes such a root only
+// to ~sqrt(eps): Newton steps become rounding noise over rounding noise and
+// x can land anywhere, and the adjugate behind the Rayleigh polish is noise
+// too (an FP32 emulation of this routine gave errors up to 0.5 nm on 2-atom
+// pairs and NaN on exact collinear copies).  Two tests, both a posteriori:
+//   * Newton did not converge (30 steps, last step above 1e-5, or NaN);
+//   * the polish's own error estimate is too large for the pair's rmsd: the
+//     polish removes an error ~dx from x and leaves ~dx^2 / gap, gap ~
+//     P'(x) / (P''(x) / 2), so rmsd error ~ lam0 dx^2 |P''/2| / (n |P'| r).
+//   * M has rank ~1 and the pair's rmsd is small against the structures'
+//     size (below).
+// The caller sends such pairs to the exact FP64 refinement, whose QCP
+// handles double roots.  In the same emulation (3,000 sampled pairs each of
+// 2,000-atom metastable, 300-atom chain and 100-atom cube frames; 1,500 each
+// of 3- to 2,000-atom collinear and nearly collinear frames with 0.01-0.2 nm
+// noise) the three tests together flagged every pair off by more than
+// 2e-5 nm and none of the generic pairs.
+__device__ __forceinline__ float qcp_msd_f32(const float (&m)[9], float ga, float gb, float inv_n,
+                                             bool& unresolved) {
+  unresolved = false;
   const float lam0 = rn_mul(0.5f, rn_add(ga, gb));
   if (!(lam0 > 0.f)) return 0.f;
   const float inv = __fdiv_rn(1.0f, lam0);
@@ -72,8 +95,23 @@ __device__ __forceinline__ float qcp_msd_f32(const float (&m)[9], float ga, floa
 #pragma unroll
   for (int t = 0; t < 9; ++t) c2 = rn_fma(mm[t], mm[t], c2);
   c2 = rn_mul(c2, -2.f);
-  const float detm = rn_dot3(mm[0], rn_det2(mm[4], mm[8], mm[5], mm[7]), -mm[1], rn_det2(mm[3], mm[8], mm[5], mm[6]),
-                             mm[2], rn_det2(mm[3], mm[7], mm[4], mm[6]));
+  const float cf00 = rn_det2(mm[4], mm[8], mm[5], mm[7]), cf01 = rn_det2(mm[3], mm[8], mm[5], mm[6]);
+  const float cf02 = rn_det2(mm[3], mm[7], mm[4], mm[6]);
+  const float detm = rn_dot3(mm[0], cf00, -mm[1], cf01, mm[2], cf02);
+  // |cof M|_F^2 = s1^2 s2^2 + s1^2 s3^2 + s2^2 s3^2 (singular values of M):
+  // near 0 when M has rank ~1, i.e. when a structure is (nearly) collinear
+  float cof2 = rn_fma(cf02, cf02, rn_fma(cf01, cf01, rn_mul(cf00, cf00)));
+  {
+    const float c10 = rn_det2(mm[1], mm[8], mm[2], mm[7]), c11 = rn_det2(mm[0], mm[8], mm[2], mm[6]);
+    const float c12 = rn_det2(mm[0], mm[7], mm[1], mm[6]), c20 = rn_det2(mm[1], mm[5], mm[2], mm[4]);
+    const float c21 = rn_det2(mm[0], mm[5], mm[2], mm[3]), c22 = rn_det2(mm[0], mm[4], mm[1], mm[3]);
+    cof2 = rn_fma(c10, c10, cof2);
+    cof2 = rn_fma(c11, c11, cof2);
+    cof2 = rn_fma(c12, c12, cof2);
+    cof2 = rn_fma(c20, c20, cof2);
+    cof2 = rn_fma(c21, c21, cof2);
+    cof2 = rn_fma(c22, c22, cof2);
+  }
   const float c1 = rn_mul(-8.f, detm);
   const float s01 = rn_det2(k00, k11, k01, k01), s02 = rn_det2(k00, k12, k02, k01), s03 = rn_det2(k00, k13, k03, k01);
   const float s12 = rn_det2(k01, k12, k02, k11), s13 = rn_det2(k01, k13, k03, k11), s23 = rn_det2(k02, k13, k03, k12);
@@ -92,6 +130,8 @@ __device__ __forceinline__ float qcp_msd_f32(const float (&m)[9], float ga, floa
   // rounding.  Far-apart structures start much closer: 17.9 -> 6.2
   // iterations on the all-pairs workload in an FP32 emulation, same errors.
   float x = fminf(1.0f, rn_mul(sqrtf(rn_mul(-1.5f, c2)), 1.00000095f));
+  float last = 0.f;      // last Newton step
+  bool converged = false;
 #pragma unroll 1
   for (int it = 0; it < 30; ++it) {
     const float x2 = rn_mul(x, x);
@@ -102,8 +142,23 @@ __device__ __forceinline__ float qcp_msd_f32(const float (&m)[9], float ga, floa
     if (!(dp != 0.0f)) break;
     const float step = __fdividef(pv, dp);
     x = rn_sub(x, step);
-    if (!(fabsf(step) > 2e-7f)) break;
+    last = step;
+    if (fabsf(step) <= 2e-7f) {  // false for NaN: a NaN step runs to the cap
+      converged = true;
+      break;
+    }
   }
+  unresolved = !converged && !(fabsf(last) <= 1e-5f);
+  // P'(x) and P''(x) / 2 at Newton's x, for the polish's error estimate
+  float slope, curv;
+  {
+    const float x2 = rn_mul(x, x);
+    const float b = rn_mul(rn_add(x2, c2), x);
+    const float a = rn_add(b, c1);
+    slope = fabsf(rn_add(rn_fma(rn_mul(2.0f, x2), x, b), a));
+    curv = fabsf(rn_fma(6.0f, x2, c2));
+  }
+  float dx = 0.f;
   // The quartic's largest root is ill-conditioned when the top eigenvalues of
   // K are close (far-apart structures): FP32 Newton stalls ~1e-6 away from it.
   // The eigenvalue itself is well-conditioned, so polish x with the Rayleigh
@@ -152,11 +207,24 @@ __device__ __forceinline__ float qcp_msd_f32(const float (&m)[9], float ga, floa
     const float bv2 = rn_dot4(b02, v0, b12, v1, b22, v2, b23, v3);
     const float bv3 = rn_dot4(b03, v0, b13, v1, b23, v2, b33, v3);
     const float vv = rn_dot4(v0, v0, v1, v1, v2, v2, v3, v3);
-    const float dx = __fdiv_rn(rn_dot4(v0, bv0, v1, bv1, v2, bv2, v3, bv3), vv);
+    dx = __fdiv_rn(rn_dot4(v0, bv0, v1, bv1, v2, bv2, v3, bv3), vv);
     if (vv > 1e-30f && fabsf(dx) < 1e-3f) x = rn_add(x, dx);
   }
-  const float msd = rn_mul(rn_mul(rn_mul(2.0f, lam0), rn_sub(1.0f, x)), inv_n);
-  return msd > 0.f ? msd : 0.f;
+  float msd = rn_mul(rn_mul(rn_mul(2.0f, lam0), rn_sub(1.0f, x)), inv_n);
+  msd = msd > 0.f ? msd : 0.f;
+  // rmsd error estimate lam0 dx^2 curv / (n slope r) <= 2e-5 nm, without a
+  // division (false for NaN or an infinite dx: such pairs are refined too)
+  const float lhs = rn_mul(rn_mul(rn_mul(lam0, inv_n), rn_mul(dx, dx)), curv);
+  const float rhs = rn_mul(rn_mul(2e-5f, sqrtf(msd)), slope);
+  if (!(lhs <= rhs)) unresolved = true;
+  // M of rank ~1 (q = |cof M|^2 / |M|_F^4 small) with an rmsd small against
+  // the structures' size: q (r / scale)^2 < 2e-7, scale = lam0 / n.  The
+  // emulation needed 1e-7 to catch every pair off by more than 2e-5 nm, and
+  // the first generic pair (300-atom chains) came at 1e-6.
+  const float i1 = rn_mul(-0.5f, c2);  // |M|_F^2 of the normalised M
+  const float sc = rn_mul(lam0, inv_n);
+  if (!(rn_mul(cof2, msd) >= rn_mul(rn_mul(2e-7f, rn_mul(i1, i1)), rn_mul(sc, sc)))) unresolved = true;
+  return msd;
 }
 
 // Refinement threshold of a pair: r < 0.25 * scale * sqrt(1/n), scale =
@@ -179,11 +247,12 @@ __device__ __forceinline__ void pair_epilogue(int64_t i, int64_t j, const float 
     return;
   }
   const float ga = (float)G[i], gb = (float)G[j];
-  const float msd = qcp_msd_f32(m, ga, gb, inv_n);
+  bool unresolved;
+  const float msd = qcp_msd_f32(m, ga, gb, inv_n, unresolved);
   const float r = sqrtf(msd);
   out[i * F + j] = r;
   out[j * F + i] = r;
-  if (pair_needs_refine(r, ga, gb, inv_n)) {
+  if (unresolved || pair_needs_refine(r, ga, gb, inv_n)) {
     const int slot = atomicAdd(rc, 1);
     if (slot < rcap)
       rl[slot] = PairRefine{(int32_t)i, (int32_t)j};
@@ -222,10 +291,11 @@ __device__ __forceinline__ CrossCol cross_col(const gbrmsd_cross_request_t* __re
 // the same refinement rule as pair_epilogue.
 __device__ __forceinline__ void cross_pair(int64_t i, int64_t j, const float (&m)[9], float ga, float gb,
                                            float inv_n, float* dst, PairRefine* rl, int* rc, int rcap, int* err) {
-  const float msd = qcp_msd_f32(m, ga, gb, inv_n);
+  bool unresolved;
+  const float msd = qcp_msd_f32(m, ga, gb, inv_n, unresolved);
   const float r = sqrtf(msd);
   *dst = r;
-  if (pair_needs_refine(r, ga, gb, inv_n)) {
+  if (unresolved || pair_needs_refine(r, ga, gb, inv_n)) {
     const int slot = atomicAdd(rc, 1);
     if (slot < rcap)
       rl[slot] = PairRefine{(int32_t)i, (int32_t)j};

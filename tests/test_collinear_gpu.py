@@ -50,3 +50,51 @@ def test_superpose_collinear_frames(cuda):
     t = md.Trajectory(x.copy())
     t.superpose(md.Trajectory(x[:1].copy()), frame=0)
     assert np.abs(t.xyz - x[0]).max() < 2e-5
+
+
+def _pairs_fp64(x):
+    F = x.shape[0]
+    iu = np.triu_indices(F, 1)
+    v = fp64.kabsch_rmsd_pairs(x, np.stack(iu, 1))
+    want = np.zeros((F, F))
+    want[iu] = v
+    want[(iu[1], iu[0])] = v
+    return want
+
+
+@pytest.mark.parametrize("method", ["tensor", "fp32"])
+@pytest.mark.parametrize("A", [2, 3, 40, 300])
+def test_allpairs_tile_epilogue_at_double_roots(cuda, method, A):
+    """Every 2-atom pair, and every pair with a collinear structure in it, has
+    a double largest eigenvalue of K; the tiles' FP32 Newton cannot resolve it
+    and hands the pair to the exact refinement."""
+    x = _frames(A, 160, seed=100 + A, sigma=0.01)
+    got = md.allpairs_rmsd(x, method=method)
+    assert_parity(got.ravel(), _pairs_fp64(x).ravel(), what=f"all-pairs {method} collinear A={A}")
+    sub = got[::4][:, ::4]  # exact rotated copies of frame 0, hence of each other
+    assert np.abs(sub).max() < 1e-5, sub.max()
+
+
+@pytest.mark.parametrize("method", ["tensor", "fp32"])
+def test_allpairs_two_atom_random_frames(cuda, method):
+    rng = np.random.default_rng(5)
+    base = rng.uniform(0, 3, (2, 3))
+    x = (base[None] + rng.normal(0, 0.1, (120, 2, 3))).astype(np.float32)
+    got = md.allpairs_rmsd(x, method=method)
+    assert_parity(got.ravel(), _pairs_fp64(x).ravel(), what=f"all-pairs {method} 2 atoms")
+
+
+@pytest.mark.parametrize("method", ["tensor", "fp32"])
+def test_cross_tile_epilogue_at_double_roots(cuda, method):
+    from mdtraj_gb300 import serving
+
+    for A in (2, 40):
+        db = _frames(A, 300, seed=200 + A, sigma=0.01)
+        queries = _frames(A, 24, seed=300 + A, sigma=0.01)
+        queries[0] = db[0]  # an exact copy of a database frame
+        server = serving.RmsdServer(db, method=method, query_capacity=64, slots=1)
+        done = server.serve([serving.Request(queries=queries, db0=0, db1=300, rid=0)], realtime=False)
+        got = done[0].result
+        want = np.stack([fp64.kabsch_rmsd(db, q) for q in queries])
+        assert_parity(got.ravel(), want.ravel(), what=f"cross {method} collinear A={A}")
+        assert abs(got[0, 0]) < 1e-5
