@@ -34,8 +34,13 @@ import numpy as np
 import torch
 
 from . import _device as D
+from . import _lib
 from ._lib import lib
-from .cross import CrossWorkspace, FrameSet, cross_launch, cross_status, request_table
+from .cross import CrossWorkspace, FrameSet, cross_launch, request_table
+
+# bumped by Request.cancel(): the loop looks for withdrawn requests only when
+# it has changed since its last look
+_CANCELS = [0]
 
 
 @dataclass
@@ -48,11 +53,14 @@ class Request:
     arrival: float = 0.0  # seconds after the start of serve()
     rid: int = -1
     result: np.ndarray | None = None  # (Q, db1 - db0) float32 once done
+    timeout: float | None = None  # seconds after arrival; None: no limit
+    status: str = "pending"  # "done", "cancelled" or "timed_out" once finished
     t_admit: float = math.nan
     t_launch: float = math.nan
     t_done: float = math.nan
     batch: int = -1
     refined: int = 0
+    _cancel: bool = field(default=False, repr=False)
     _p0: int = field(default=-1, repr=False)
     _out: torch.Tensor | None = field(default=None, repr=False)
     _host: torch.Tensor | None = field(default=None, repr=False)
@@ -69,6 +77,17 @@ class Request:
     @property
     def latency(self) -> float:
         return self.t_done - self.arrival
+
+    def cancel(self) -> None:
+        """Withdraws the request (from any thread).  While it is queued or
+        admitted it is dropped before launch; once its batch is on the GPU
+        the batch runs to the end and its result is discarded.  Either way
+        it finishes with status "cancelled" and no result."""
+        self._cancel = True
+        _CANCELS[0] += 1
+
+    def expired(self, now: float) -> bool:
+        return self.timeout is not None and now > self.arrival + self.timeout
 
 
 class PoolAllocator:
@@ -157,6 +176,33 @@ class HostResultPool:
             pass
 
 
+class QueryStaging:
+    """Page-locked host rows mirroring the device query pool: a request's
+    query frames are copied (host memcpy) into the rows of its pool slot and
+    go up with an asynchronous copy.  torch's copy from the caller's pageable
+    array waits on the host until the copy engine has taken it, which behind
+    a batch's result copies to the host took ~0.8 ms per request (a third of
+    the loop's time in a 300-request burst)."""
+
+    def __init__(self, rows: int, row_floats: int):
+        self.arr = np.empty((int(rows), int(row_floats)), dtype=np.float32)
+        self.locked = lib.gbrmsd_host_register(self.arr.ctypes.data, self.arr.nbytes) == 0
+
+    def ptr(self, row: int) -> int:
+        return self.arr.ctypes.data + int(row) * self.arr.strides[0]
+
+    def close(self) -> None:
+        if self.locked:
+            lib.gbrmsd_host_unregister(self.arr.ctypes.data)
+            self.locked = False
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class _Slot:
     def __init__(self, device):
         self.stream = torch.cuda.Stream(device=device)
@@ -164,6 +210,9 @@ class _Slot:
         self.event = None
         self.batch = None
         self.ws_buf = None
+        # the batch's error word and refined-pair count, copied to the host
+        # right after its kernels (read once its event has fired)
+        self.hdr = torch.zeros(2, dtype=torch.int32, pin_memory=True)
 
 
 class RmsdServer:
@@ -193,6 +242,7 @@ class RmsdServer:
         self.qcap = int(query_capacity)
         self.qset = FrameSet(self.qcap, self.n_atoms, self.device)
         self.staging = torch.empty((self.qcap, 3 * self.n_atoms), dtype=torch.float32, device=self.device)
+        self.qhost = QueryStaging(self.qcap, 3 * self.n_atoms)
         self.pool = PoolAllocator(self.qcap)
         self.budget = int(hbm_budget_bytes)
         self.used = 0
@@ -265,11 +315,20 @@ class RmsdServer:
         with torch.cuda.stream(s):
             for r in batch:
                 rows = self.staging[r._p0:r._p0 + r.n_query]
-                rows.copy_(torch.from_numpy(r.queries.reshape(r.n_query, -1)), non_blocking=True)
+                q = r.queries.reshape(r.n_query, -1)
+                if self.qhost.locked:
+                    # rows of a pool slot are not reused before the batch
+                    # holding them completes, so the host rows are free too
+                    self.qhost.arr[r._p0:r._p0 + r.n_query] = q
+                    nb = q.nbytes
+                    D.copy_rows(rows.data_ptr(), nb, self.qhost.ptr(r._p0), nb, nb, 1, 1, s.cuda_stream)
+                else:
+                    rows.copy_(torch.from_numpy(q), non_blocking=True)
                 self.qset.prepare(rows, r._p0, stream=s.cuda_stream)
             table = request_table([(r._out.data_ptr(), r._p0, r.n_query, r.db0, r.db1) for r in batch])
             ws = slot.ws.get(self.n_db, self.qcap, len(batch))
             cross_launch(self.db, self.n_db, self.qset, table, len(batch), self.method, ws, s.cuda_stream)
+            slot.hdr.copy_(ws[:8].view(torch.int32), non_blocking=True)
             if self.result_to_host:
                 for r in batch:
                     nb = 4 * r._out.numel()
@@ -287,11 +346,47 @@ class RmsdServer:
         self.batch_sizes.append(len(batch))
         slot.event, slot.batch, slot.ws_buf = ev, batch, ws
 
+    def _unadmit(self, r: Request) -> None:
+        """Returns an admitted, not launched request's pool rows, budget and
+        host result pages."""
+        if r._hoff >= 0:
+            self.hpool.release(r._hoff, r.result_bytes)
+            r._hoff = -1
+        self.pool.release(r._p0, r.n_query)
+        self.used -= r.result_bytes
+        r._out = None
+
+    @staticmethod
+    def _drop(r: Request, status: str, now: float) -> Request:
+        r.status = status
+        r.result = None
+        r.t_done = now
+        return r
+
     def _complete(self, slot: _Slot, now: float, keep_results: bool) -> list:
-        refined = cross_status(slot.ws_buf, slot.stream.cuda_stream)  # raises on a device error
+        err, refined = (int(v) for v in slot.hdr.tolist())  # copied before the batch's event
+        if err:
+            raise _lib.GbrmsdError(_lib.E_DEVICE, "cross RMSD batch: device error word 0x%x (1 = wait expired, "
+                                                  "4 = refinement list full)" % err)
         done = slot.batch
         for r in done:
             shape = (r.n_query, r.db1 - r.db0)
+            # a request withdrawn or out of time while its batch ran: the
+            # batch has finished, so its memory is released and the result
+            # discarded
+            late = "cancelled" if r._cancel else ("timed_out" if r.expired(now) else None)
+            if late is not None:
+                if r._hoff >= 0:
+                    self.hpool.release(r._hoff, r.result_bytes)
+                    r._hoff = -1
+                self.pool.release(r._p0, r.n_query)
+                self.used -= r.result_bytes
+                r._out = None
+                r._host = None
+                r.refined = refined
+                self._drop(r, late, now)
+                continue
+            r.status = "done"
             if self.result_to_host and r._hoff >= 0:
                 if keep_results:
                     # an array over pool pages; they return when it is dropped
@@ -327,6 +422,8 @@ class RmsdServer:
         batch_bytes = 0
         batch_cap = (self.hpool.buf.nbytes // len(self.slots)) if self.hpool is not None and self.hpool.locked else 0
         nxt = 0
+        has_timeouts = any(r.timeout is not None for r in reqs)
+        cancels_seen, last_scan = -1, -1.0
         t0 = time.perf_counter()
         while len(finished) < n:
             now = time.perf_counter() - t0
@@ -336,6 +433,29 @@ class RmsdServer:
             for slot in self.slots:
                 if slot.event is not None and slot.event.query():
                     finished.extend(self._complete(slot, time.perf_counter() - t0, keep_results))
+            # requests withdrawn or out of time before their launch leave now
+            # (looked for when a cancel happened, and every ms with timeouts)
+            scan = _CANCELS[0] != cancels_seen or (has_timeouts and now - last_scan > 1e-3)
+            if scan:
+                cancels_seen, last_scan = _CANCELS[0], now
+            if scan and any(r._cancel or r.expired(now) for r in queue):
+                keep = deque()
+                for r in queue:
+                    if r._cancel or r.expired(now):
+                        finished.append(self._drop(r, "cancelled" if r._cancel else "timed_out", now))
+                    else:
+                        keep.append(r)
+                queue = keep
+            if scan and any(r._cancel or r.expired(now) for r in admitted):
+                keep = []
+                for r in admitted:
+                    if r._cancel or r.expired(now):
+                        self._unadmit(r)
+                        batch_bytes -= r.result_bytes
+                        finished.append(self._drop(r, "cancelled" if r._cancel else "timed_out", now))
+                    else:
+                        keep.append(r)
+                admitted = keep
             idle = not admitted and all(s.event is None for s in self.slots)
             while queue and (self.max_batch is None or len(admitted) < self.max_batch):
                 # a batch holds at most 1/slots of the host result pool, so
@@ -364,7 +484,9 @@ class RmsdServer:
 
 
 def latency_summary(done: list, t_first: float | None = None) -> dict:
-    """p50 / p99 / mean latency (ms) and completed queries per second."""
+    """p50 / p99 / mean latency (ms) and completed queries per second, over
+    the requests that finished with a result (status "done")."""
+    done = [r for r in done if r.status == "done"]
     lat = np.array([r.latency for r in done]) * 1e3
     t0 = min(r.arrival for r in done) if t_first is None else t_first
     t1 = max(r.t_done for r in done)

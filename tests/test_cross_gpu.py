@@ -162,3 +162,44 @@ def test_serving_budget_gates_admission(cuda):
         assert_parity(r.result.ravel(), oracle_block(db, r.queries, r.db0, r.db1).ravel(), what=f"request {r.rid}")
     s = serving.latency_summary(done)
     assert s["requests"] == len(reqs) and s["p99_ms"] >= s["p50_ms"] > 0
+
+
+def test_serving_cancel_and_timeout(cuda):
+    """Requests withdrawn or out of time finish without a result, whether it
+    happens while they are queued or while their batch is on the GPU; their
+    memory is returned and every other request's result is unchanged."""
+    db = chain_db(2000, 300, seed=8)
+    dbs = cross.FrameSet.from_frames(db)
+    reqs = make_requests(db, 16, seed=9)
+    alone_server = serving.RmsdServer(dbs, method="tensor", query_capacity=1024, slots=1, max_batch_requests=1)
+    alone = {r.rid: r.result for r in alone_server.serve(clone(reqs), realtime=False)}
+
+    cancel_in_flight, late_in_flight = 5, 9
+
+    class Server(serving.RmsdServer):
+        def _launch(self, slot, batch, now):
+            super()._launch(slot, batch, now)
+            for r in batch:
+                if r.rid == cancel_in_flight:
+                    r.cancel()                     # withdrawn while its batch runs
+                if r.rid == late_in_flight:
+                    r.timeout = now - r.arrival    # runs out while its batch runs
+
+    server = Server(dbs, method="tensor", query_capacity=1024, slots=2, max_batch_requests=4)
+    work = clone(reqs)
+    work[2].cancel()                # withdrawn before it is queued
+    work[7].timeout = 1e-9          # out of time while queued
+    done = {r.rid: r for r in server.serve(work, realtime=False)}
+    assert len(done) == len(reqs)
+    want = {2: "cancelled", 7: "timed_out", cancel_in_flight: "cancelled", late_in_flight: "timed_out"}
+    for rid, r in done.items():
+        assert r.status == want.get(rid, "done"), (rid, r.status)
+        if rid in want:
+            assert r.result is None
+        else:
+            np.testing.assert_array_equal(r.result, alone[rid], err_msg=f"request {rid}")
+    assert done[cancel_in_flight].batch >= 0 and done[late_in_flight].batch >= 0
+    assert done[2].batch == -1 and done[7].batch == -1
+    assert server.used == 0 and server.pool.free_rows == 1024
+    s = serving.latency_summary(list(done.values()))
+    assert s["requests"] == len(reqs) - len(want)
