@@ -1,9 +1,12 @@
-"""Multi-rank host logic of the benchmark (frame sharding, max-over-ranks
-timing) on two gloo ranks on the CPU: frames shard with no data-path
-collective; the only collective is the MAX of the per-rank timings."""
+"""Multi-rank host logic on gloo ranks on the CPU: the benchmark's frame
+sharding and max-over-ranks timing (frames shard with no data-path
+collective; the only collective is the MAX of the per-rank timings), and
+the product's sharded md.rmsd (mdtraj_gb300.shard), whose gathered result
+must equal one call over all frames bit for bit."""
 import os
 import socket
 
+import numpy as np
 import pytest
 
 torch = pytest.importorskip("torch")
@@ -51,3 +54,82 @@ def test_two_gloo_ranks_shard_and_time():
     assert (r0, r1, w0, w1, l0, l1) == (0, 1, 2, 2, 0, 1)
     assert (a0, b0, a1, b1) == (0, 1000, 1000, 2000)  # weak scaling: disjoint, equal per-rank work
     assert s0 == s1 == 2.5                             # every rank reports the slowest rank's time
+
+
+def _oracle_score(t, r, frame, **kw):
+    """md.rmsd's CPU path of the reference (compiled reference, or the C
+    restatement) on one rank's frames; centres them in place like md.rmsd."""
+    from oracle import cpu
+
+    impl = cpu.best_available()
+    return impl.md_rmsd(t.xyz, np.ascontiguousarray(r.xyz[frame]).copy())
+
+
+class _Traj:
+    def __init__(self, xyz):
+        self.xyz = xyz
+        self._rmsd_traces = None
+
+
+def _shard_worker(rank, world, port, q):
+    import torch.distributed as dist
+
+    from mdtraj_gb300 import synth
+    from mdtraj_gb300.shard import frame_range, rmsd_sharded
+
+    os.environ.update({"MASTER_ADDR": "127.0.0.1", "MASTER_PORT": str(port)})
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        _, x = synth.single_reference_frames(1001, 57, seed=11, sigma=np.geomspace(1e-3, 0.3, 1001),
+                                             exact_fraction=0.02)
+        t = _Traj(x)
+        out = rmsd_sharded(t, _Traj(x.copy()), 3, score=_oracle_score)
+        f0, f1 = frame_range(1001, rank, world)
+        q.put((rank, out, f0, f1, t.xyz[f0:f1].copy()))
+    finally:
+        dist.destroy_process_group()
+
+
+@pytest.mark.parametrize("world", [2, 3])
+def test_rmsd_sharded_over_gloo_ranks_equals_one_call(world):
+    """Each rank scores its own frame range, the (F,) results are gathered
+    once, and the gathered array equals one md.rmsd over all frames bit for
+    bit; each rank's in-place centring of its frames equals the one call's."""
+    import torch.multiprocessing as mp
+
+    from mdtraj_gb300 import synth
+    from mdtraj_gb300.shard import frame_range
+
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_shard_worker, args=(r, world, port, q)) for r in range(world)]
+    for p in procs:
+        p.start()
+    res = sorted((q.get(timeout=180) for _ in range(world)), key=lambda v: v[0])
+    for p in procs:
+        p.join(60)
+    assert all(p.exitcode == 0 for p in procs), [p.exitcode for p in procs]
+    _, x = synth.single_reference_frames(1001, 57, seed=11, sigma=np.geomspace(1e-3, 0.3, 1001), exact_fraction=0.02)
+    whole = _Traj(x)
+    want = _oracle_score(whole, _Traj(x.copy()), 3)
+    sizes = [f1 - f0 for _, _, f0, f1, _ in res]
+    assert sum(sizes) == 1001 and max(sizes) - min(sizes) <= 1
+    for rank, out, f0, f1, centred in res:
+        assert (f0, f1) == frame_range(1001, rank, world)
+        np.testing.assert_array_equal(out, want)
+        np.testing.assert_array_equal(centred, whole.xyz[f0:f1])
+
+
+def test_frame_range_covers_frames_once():
+    from mdtraj_gb300.shard import frame_range
+
+    for n in (0, 1, 7, 1000, 1001):
+        for w in (1, 2, 3, 8):
+            seen = np.zeros(n, int)
+            for r in range(w):
+                a, b = frame_range(n, r, w)
+                seen[a:b] += 1
+            assert np.all(seen == 1)
+    with pytest.raises(ValueError):
+        frame_range(10, 2, 2)
