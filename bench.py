@@ -184,8 +184,55 @@ def max_over_ranks(value: float, world: int) -> float:
 # ---------------------------------------------------------------------------
 
 
+def _synth():
+    """mdtraj_gb300/synth.py (numpy-only generators) loaded as a standalone
+    module: importing it through the package would load libgbrmsd.so, and
+    the reference arm must not map any of this project's libraries."""
+    import importlib.util
+
+    name = "_bench_synth"
+    if name not in sys.modules:
+        spec = importlib.util.spec_from_file_location(name, ROOT / "mdtraj_gb300" / "synth.py")
+        mod = importlib.util.module_from_spec(spec)
+        sys.modules[name] = mod
+        spec.loader.exec_module(mod)
+    return sys.modules[name]
+
+
+def _padded(n_atoms: int) -> int:
+    return (int(n_atoms) + 3) // 4 * 4
+
+
+def workload_config(workload: str, n_frames: int, world: int) -> dict:
+    """The `config` object of both arms (this project's and the reference's):
+    the same keys and values, so that the two lines name one workload.  How
+    each arm runs it (device layout, OpenMP threads) is stated outside
+    `config`."""
+    spec = WORKLOADS[workload]
+    if workload.startswith("allpairs"):
+        _, A, C, sig, cube, stay = spec
+        F = n_frames
+        return {"workload": workload, "n_frames": F, "n_atoms": A, "centres": C, "sigma_nm": sig,
+                "output": "full symmetric %d x %d float32" % (F, F),
+                "l2": "operands (%.2f GB BF16 hi+lo) and output (%.2f GB) larger than L2; no flush"
+                      % (3.0 * F * ((A + 63) // 64 * 64) * 2 * 2 / 1e9, 4.0 * F * F / 1e9),
+                "parallelism": f"frame shards x{world}"}
+    _, A, layout, s_lo, s_hi, exact = spec
+    F = n_frames
+    nbytes = 12.0 * _padded(A) * F
+    small = nbytes < 4 * L2_BYTES
+    return {"workload": workload, "n_frames": F, "n_atoms": A, "precentered": False,
+            "sigma_nm": [s_lo, s_hi], "exact_copy_fraction": exact,
+            "layout": ("%s float32 frames resident in HBM (value); host float32 (F, A, 3) atom-major arrays "
+                       "(e2e and the reference's md.rmsd)" % ("axis-major" if layout == 1 else "atom-major")),
+            "l2": ("inputs (%.3f GB) fit in L2: 256 MB write + 256 MB read between steps, each step timed alone, "
+                   "launches replayed from a CUDA graph" % (nbytes / 1e9)) if small else
+                  "inputs (%.1f GB) larger than L2; no flush" % (nbytes / 1e9),
+            "parallelism": f"frame shards x{world}"}
+
+
 def cpu_sample(n_atoms: int, n_sample: int, seed: int, sigma_lo: float, sigma_hi: float):
-    from mdtraj_gb300 import synth
+    synth = _synth()
 
     rng = np.random.default_rng(seed)
     sig = synth.log_uniform(rng, sigma_lo, sigma_hi, n_sample) if sigma_lo != sigma_hi else sigma_lo
@@ -345,6 +392,9 @@ def run_gpu(args) -> dict:
         cpu_base = time_cpu_reference(A, args.cpu_budget, s_lo, s_hi)
 
     clocks = clk.summary()
+    workloads = None
+    if rank == 0 and world == 1 and args.workload == DEFAULT_WORKLOAD and not args.skip_workloads:
+        workloads = run_workloads(args)
     return {
         "metric": "rmsd_frames_per_s",
         "value": round(value, 1),
@@ -358,20 +408,65 @@ def run_gpu(args) -> dict:
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded, generated on device)",
-        "config": {"workload": args.workload, "n_frames": F, "n_atoms": A,
-                   "layout": "axis-major" if layout == 1 else "atom-major", "precentered": False,
-                   "sigma_nm": [s_lo, s_hi], "exact_copy_fraction": exact,
-                   "l2": ("inputs (%.3f GB) fit in L2: 256 MB write + 256 MB read between steps, each step timed alone, "
-                          "launches replayed from a CUDA graph" % (12.0 * Ap * F / 1e9)) if small else
-                         "inputs (%.1f GB) larger than L2; no flush" % (12.0 * Ap * F / 1e9),
-                   "parallelism": f"frame shards x{world}"},
+        "config": workload_config(args.workload, F, world),
         "roofline": roof,
         "cpu_baseline": cpu_base,
         "e2e": e2e,
         "gpu_launches": 3 * args.steps,
         "clocks": clocks,
         "accuracy": acc,
+        "workloads": workloads,
     }
+
+
+def run_workloads(args) -> dict:
+    """The other benchmark workloads, each shortened to a few seconds, run
+    after the headline workload's own timed region so that one default run
+    carries evidence for all of them (each entry has its own clock record):
+      cfg0 single_reference_10000x1000  md.rmsd's class of input: graph-replayed
+           step, streaming-kernel roofline, accuracy vs FP64 and the reference;
+      cfg2 allpairs_20000x2000  tensor-core matrix vs the FP32 CUDA-core tiles
+           (ratio), 100,000 sampled pairs vs FP64;
+      cfg3 ragged_512  one persistent graph launch vs 512 separate launches;
+      cfg4 serving_500000x300  p50/p99 and queries/s at 100, 1,000 and 10,000
+           offered requests/s beside one request per launch on FP32 tiles
+           (fewer requests per rate than the full sweep of --workload
+           serving_500000x300)."""
+    import torch
+
+    def sub(workload, fn, **kw):
+        ns = argparse.Namespace(**vars(args))
+        ns.workload, ns.frames, ns.skip_e2e, ns.skip_cpu, ns.warmup = workload, None, True, True, 3
+        for k, v in kw.items():
+            setattr(ns, k, v)
+        t0 = time.perf_counter()
+        try:
+            r = fn(ns)
+        except Exception as exc:  # one workload failing must not take the headline line with it
+            r = {"error": f"{type(exc).__name__}: {exc}"[:400]}
+        r["wall_s"] = round(time.perf_counter() - t0, 1)
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+        return r
+
+    def keep(r, keys):
+        return {k: r[k] for k in keys if k in r}
+
+    out = {}
+    r = sub("single_reference_10000x1000", run_gpu, steps=20)
+    out["cfg0_single_reference_10000x1000"] = keep(r, ["value", "unit", "ms_per_step", "steps", "roofline", "accuracy",
+                                                       "clocks", "config", "error", "wall_s"])
+    r = sub("allpairs_20000x2000", run_allpairs, steps=3)
+    out["cfg2_allpairs_20000x2000"] = keep(r, ["value", "unit", "ms_per_step", "steps", "roofline", "fp32_cuda_core",
+                                               "refined_pairs", "accuracy", "clocks", "config", "error", "wall_s"])
+    r = sub("ragged_512", run_ragged, steps=3)
+    out["cfg3_ragged_512"] = keep(r, ["value", "unit", "ms_per_step", "steps", "roofline", "separate_launches",
+                                      "accuracy", "clocks", "config", "error", "wall_s"])
+    r = sub("serving_500000x300", run_serving, rates=(100, 1000, 10000), serve_seconds=1.0, serve_max=400,
+            baseline_max=100)
+    out["cfg4_serving_500000x300"] = keep(r, ["value", "unit", "sweep", "speedup_at_top_rate", "roofline",
+                                              "kernel_compare", "accuracy", "clocks", "config", "error", "wall_s"])
+    return out
 
 
 def accuracy_check(x, ref, out, F, A, Ap, layout, sig, rank) -> dict:
@@ -389,14 +484,34 @@ def accuracy_check(x, ref, out, F, A, Ap, layout, sig, rank) -> dict:
         fr = sel[:, :, :A].transpose(1, 2).contiguous().cpu().numpy()
     else:
         fr = sel.view(len(idx), Ap, 3)[:, :A].contiguous().cpu().numpy()
-    want = fp64.kabsch_rmsd(fr, ref.cpu().numpy())
+    ref_h = ref.cpu().numpy()
+    want = fp64.kabsch_rmsd(fr, ref_h)
     got = out[torch.from_numpy(idx).to(out.device)].cpu().numpy().astype(np.float64)
     err = np.abs(got - want)
     ex = np.isin(idx, exact_idx)
-    return {"checked_frames": int(len(idx)), "exact_copies": int(ex.sum()),
-            "max_err_nm": float(err.max()), "rms_err_nm": float(np.sqrt((err ** 2).mean())),
-            "max_err_exact_copies_nm": float(err[ex].max()) if ex.any() else None,
-            "oracle": "FP64 Kabsch/SVD (oracle/fp64.py)"}
+    res = {"checked_frames": int(len(idx)), "exact_copies": int(ex.sum()),
+           "max_err_nm": float(err.max()), "rms_err_nm": float(np.sqrt((err ** 2).mean())),
+           "max_err_exact_copies_nm": float(err[ex].max()) if ex.any() else None,
+           "oracle": "FP64 Kabsch/SVD (oracle/fp64.py)"}
+    # the same frames through the reference's own float32 md.rmsd (its CPU
+    # kernels compiled from its sources): the second half of the parity bar,
+    # |gpu - ref| <= 1e-4 + |ref - fp64|
+    try:
+        from oracle import cpu
+
+        impl = cpu.best_available()
+        r = impl.md_rmsd(np.ascontiguousarray(fr, dtype=np.float32), np.ascontiguousarray(ref_h, dtype=np.float32))
+        r = r.astype(np.float64)
+        ref_err = np.abs(r - want)
+        bad = np.abs(got - r) > 1e-4 + ref_err
+        res["vs_reference"] = {"kind": impl.kind, "frames_outside_bar": int(bad.sum()),
+                               "max_abs_gpu_minus_ref_nm": float(np.abs(got - r).max()),
+                               "reference_max_err_vs_fp64_nm": float(ref_err.max()),
+                               "reference_frames_off_fp64_by_more_than_1e-4": int((ref_err > 1e-4).sum()),
+                               "bar": "|gpu - ref| <= 1e-4 nm + |ref - fp64|"}
+    except (OSError, FileNotFoundError) as exc:
+        res["vs_reference"] = {"unavailable": str(exc)}
+    return res
 
 
 def run_e2e(args, F, A, s_lo, s_hi, exact, dev) -> dict:
@@ -438,12 +553,65 @@ def run_e2e(args, F, A, s_lo, s_hi, exact, dev) -> dict:
         md.rmsd(target, reference, 0)
         times.append(time.perf_counter() - t0)
     t = float(np.mean(times))
+    t_med = float(np.median(times))
     # inbound: every frame and the reference frame; outbound: one RMSD per
     # frame and the in-place centring of every frame written back
-    return {"value": round(Fe / t, 1), "unit": "frames/s", "h2d_bytes_per_step": int(Fe * A * 12 + A * 12),
-            "d2h_bytes_per_step": int(Fe * 4 + Fe * A * 12), "ms_per_step": round(t * 1e3, 2),
-            "frames": Fe, "api": "mdtraj_gb300.rmsd(target, reference, 0) on host float32 arrays",
-            "steps": args.e2e_steps, "step_ms": [round(x * 1e3, 2) for x in times]}
+    h2d, d2h = int(Fe * A * 12 + A * 12), int(Fe * 4 + Fe * A * 12)
+    link = host_link_peak(dev)
+    res = {"value": round(Fe / t, 1), "unit": "frames/s", "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": d2h, "ms_per_step": round(t * 1e3, 2),
+           "median_ms_per_step": round(t_med * 1e3, 2), "median_value": round(Fe / t_med, 1),
+           "frames": Fe, "api": "mdtraj_gb300.rmsd(target, reference, 0) on host float32 arrays",
+           "steps": args.e2e_steps, "step_ms": [round(x * 1e3, 2) for x in times], "host_link": link}
+    if link.get("both_gbs"):
+        # the step's host traffic over the link's measured two-way rate
+        res["host_link_frac"] = round((h2d + d2h) / t / 1e9 / link["both_gbs"], 4)
+        res["host_link_frac_median"] = round((h2d + d2h) / t_med / 1e9 / link["both_gbs"], 4)
+    return res
+
+
+def host_link_peak(dev, nbytes: int = 4 << 30, chunk: int = 256 << 20, reps: int = 3) -> dict:
+    """Measured host<->device rate of this machine with the copy engines:
+    `nbytes` of page-locked host memory to the device, the device to a
+    second page-locked buffer, each alone and both at once on two streams,
+    one cudaMemcpyAsync (torch copy_) per `chunk`.  Best of `reps`."""
+    import torch
+
+    try:
+        src = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+        dst = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+        d_in = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+        d_out = torch.ones(nbytes, dtype=torch.uint8, device=dev)
+    except RuntimeError as exc:
+        return {"unavailable": str(exc).splitlines()[0]}
+    s1, s2 = torch.cuda.Stream(device=dev), torch.cuda.Stream(device=dev)
+    n = nbytes // chunk
+
+    def run(h2d: bool, d2h: bool) -> float:
+        best = float("inf")
+        for _ in range(reps):
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            for k in range(n):
+                sl = slice(k * chunk, (k + 1) * chunk)
+                if h2d:
+                    with torch.cuda.stream(s1):
+                        d_in[sl].copy_(src[sl], non_blocking=True)
+                if d2h:
+                    with torch.cuda.stream(s2):
+                        dst[sl].copy_(d_out[sl], non_blocking=True)
+            torch.cuda.synchronize(dev)
+            best = min(best, time.perf_counter() - t0)
+        return best
+
+    t_in, t_out, t_both = run(True, False), run(False, True), run(True, True)
+    res = {"h2d_gbs": round(nbytes / t_in / 1e9, 1), "d2h_gbs": round(nbytes / t_out / 1e9, 1),
+           "both_gbs": round(2 * nbytes / t_both / 1e9, 1),
+           "method": "%d MB page-locked each way, %d MB cudaMemcpyAsync chunks, copy engines, best of %d"
+                     % (nbytes >> 20, chunk >> 20, reps)}
+    del src, dst, d_in, d_out
+    torch.cuda.empty_cache()
+    return res
 
 
 # ---------------------------------------------------------------------------
@@ -534,10 +702,7 @@ def run_allpairs(args) -> dict:
         "vs_baseline": None,
         "dtype": "bf16x3 (split hi/lo, f32 accumulate)",
         "data": "synthetic (seeded, generated on device)",
-        "config": {"workload": args.workload, "n_frames": F, "n_atoms": A, "centres": C, "sigma_nm": sig,
-                   "output": "full symmetric %d x %d float32" % (F, F),
-                   "l2": "operands (%.2f GB BF16 hi+lo) and output (%.2f GB) larger than L2; no flush"
-                         % (3.0 * F * ((A + 63) // 64 * 64) * 2 * 2 / 1e9, 4.0 * F * F / 1e9)},
+        "config": workload_config(args.workload, F, world),
         "roofline": roof,
         "fp32_cuda_core": {"ms_per_step": round(ms_fp32, 3), "kernel_ms": round(k_fp32, 3),
                            "pairs_per_s": round(pairs / (ms_fp32 / 1e3), 1),
@@ -572,9 +737,9 @@ def time_cpu_allpairs(A, budget_s, C, sig, cube) -> dict:
     """Reference CPU path of the clustering loop: precentered md.rmsd rows
     (getMultipleRMSDs_atom_major of the reference kernels) over a sample of
     rows of a 20,000-frame trajectory sample; pairs/s."""
-    from mdtraj_gb300 import synth
     from oracle import cpu
 
+    synth = _synth()
     impl = cpu.best_available()
     n_frames = 4000
     labels, x = synth.metastable_walk(n_frames, A, n_centres=C, seed=5, sigma=sig, cube=cube)
@@ -789,12 +954,14 @@ def run_reference(args) -> dict:
                 "unit": "pairs/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
                 "ms_per_step": round(F * (F - 1) / 2 / base["value"] * 1e3, 2), "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-                "config": {"workload": args.workload, "n_frames": F, "n_atoms": A,
-                           "note": "each step timed on a bounded row sample"},
+                "config": workload_config(args.workload, args.frames or F, world),
+                "how": "the reference's CPU kernels on all host cores; each step timed on a bounded row sample",
                 "cpu_baseline": base,
                 "e2e": {"value": round(base["value"], 1), "unit": "pairs/s", "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}}
     F, A, layout, s_lo, s_hi, exact = WORKLOADS[args.workload]
+    if args.frames:
+        F = args.frames
     base = time_cpu_reference(A, args.cpu_budget, s_lo, s_hi)
     per_step_s = F / base["value"]
     return {
@@ -811,10 +978,9 @@ def run_reference(args) -> dict:
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded)",
-        "config": {"workload": args.workload, "n_frames": F, "n_atoms": A, "layout": "atom-major (host)",
-                   "precentered": False, "sigma_nm": [s_lo, s_hi], "exact_copy_fraction": exact,
-                   "parallelism": "OpenMP over the host cores",
-                   "note": "each step timed on a bounded frame sample"},
+        "config": workload_config(args.workload, F, world),
+        "how": ("md.rmsd's CPU path (the reference's centring and msd kernels, OpenMP over all host cores) on "
+                "host atom-major arrays; each step timed on a bounded frame sample"),
         "cpu_baseline": base,
         "e2e": {"value": round(base["value"], 1), "unit": "frames/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
@@ -868,6 +1034,7 @@ def run_serving(args) -> dict:
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     F, A, rates, max_q, slice_range = WORKLOADS[args.workload]
+    rates = getattr(args, "rates", None) or rates
     if args.frames:
         F = args.frames
     t_setup = time.perf_counter()
@@ -1308,6 +1475,8 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU baseline work")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-workloads", action="store_true",
+                    help="default workload only: leave out the shortened runs of the other workloads")
     ap.add_argument("--serve-seconds", type=float, default=2.0, help="offered load per rate (seconds of arrivals)")
     ap.add_argument("--serve-max", type=int, default=1500, help="max requests per rate")
     ap.add_argument("--baseline-max", type=int, default=300, help="max requests per rate for the one-per-launch baseline")
