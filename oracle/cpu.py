@@ -29,10 +29,14 @@ _vp, _i64, _i32 = C.c_void_p, C.c_int64, C.c_int32
 
 
 def build(ref: bool = True) -> None:
-    """Builds the port (and, when its sources are available, the reference)."""
+    """Builds the port (and, when its sources are available -- the checkout
+    named by MDTRAJ_REF, or the copy staged under oracle/_ref/src -- the
+    reference)."""
     subprocess.run(["make", "-s", "-C", str(HERE), "port"], check=True)
     if ref:
-        subprocess.run(["make", "-s", "-C", str(HERE), "ref"], check=False,
+        root = os.environ.get("MDTRAJ_REF")
+        extra = [f"REF_ROOT={root}"] if root else []
+        subprocess.run(["make", "-s", "-C", str(HERE), "ref", *extra], check=False,
                        stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
 
 

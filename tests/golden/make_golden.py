@@ -1,7 +1,8 @@
 """Generates the golden fixtures in tests/golden/ from the reference itself.
 
-Run in a container that has the reference checkout (default /root/reference,
-override with MDTRAJ_REF); never on the GPU host.  It builds the reference's
+Run in a container that has the reference checkout, named by the MDTRAJ_REF
+environment variable (the directory that holds the mdtraj/ package of the
+reference project); never on the GPU host.  It builds the reference's
 own Cython RMSD extension (mdtraj/rmsd/_rmsd.pyx with its C++ kernels) and
 its XTC reader out of tree under oracle/_ref/py (git-ignored), imports them
 through a stub ``mdtraj`` package, and records:
@@ -28,7 +29,7 @@ through a stub ``mdtraj`` package, and records:
                     by the reference's XTC writer, with its reader's output
                     (coordinates, time, step, box) for the GPU decoder.
 
-Usage:  python tests/golden/make_golden.py
+Usage:  MDTRAJ_REF=<reference checkout> python tests/golden/make_golden.py
 """
 from __future__ import annotations
 
@@ -43,7 +44,9 @@ from pathlib import Path
 import numpy as np
 
 REPO = Path(__file__).resolve().parents[2]
-REF = Path(os.environ.get("MDTRAJ_REF", "/root/reference"))
+if not os.environ.get("MDTRAJ_REF"):
+    sys.exit("make_golden.py: set MDTRAJ_REF to the reference checkout (the directory holding mdtraj/)")
+REF = Path(os.environ["MDTRAJ_REF"])
 OUT = Path(__file__).resolve().parent
 BUILD = REPO / "oracle" / "_ref" / "py"
 SRC = REPO / "oracle" / "_ref" / "pysrc"
