@@ -75,6 +75,17 @@ constexpr int NEPI_THREADS = 32 * NEPI;
 constexpr int NTHREADS = 64 + NEPI_THREADS;
 constexpr int PASSES_PER_CHUNK = (CHUNK_PAIRS + NEPI_THREADS - 1) / NEPI_THREADS;  // 2
 constexpr int PASSES = NCHUNK * PASSES_PER_CHUNK;                                 // 10 per tile
+// DIRECT kernel (frames of at most DIRECT_MAX_KB k blocks, 320 atoms): no
+// accumulators in registers, so a worker needs ~72 of them and 21 worker
+// warps fit -- one thread per frame pair of a chunk (one pass per chunk, 5
+// per tile) and ~5 warps per scheduler to hide the epilogue's dependent FP32
+// chains; the first NEPI of them stage the chunks from tensor memory.
+constexpr int DIRECT_MAX_KB = 5;
+constexpr int NEPI_D = (CHUNK_PAIRS + 31) / 32;          // 21
+constexpr int NEPI_D_THREADS = 32 * NEPI_D;             // 672
+constexpr int NTHREADS_D = 64 + NEPI_D_THREADS;          // 736
+static_assert(NEPI_D_THREADS >= CHUNK_PAIRS && NEPI_D >= NEPI, "one pair per thread per chunk");
+__host__ __device__ constexpr int kernel_threads(bool direct) { return direct ? NTHREADS_D : NTHREADS; }
 constexpr uint32_t SPIN = 1u << 24;
 static_assert(EPI_COLS == NGROUP * 16, "one 16-column TMEM load per worker warp per chunk");
 static_assert(R_COL + TILE_N <= TMEM_COLS && P_COL + TILE_N <= R_COL, "TMEM layout");
@@ -216,8 +227,13 @@ __device__ __forceinline__ bool named_bar_or(int id, int n, bool v) {
   return r != 0;
 }
 
-template <bool CROSS>
-__global__ void __launch_bounds__(NTHREADS, 1) allpairs_tc_kernel(const __grid_constant__ CUtensorMap map_hi_a,
+// DIRECT: each tile accumulates all its k blocks in one of two tensor-memory
+// buffers (columns 0-239 and 256-495), alternating by tile, with no fold into
+// registers; the workers' epilogue reads the finished buffer while the MMAs
+// fill the other.  The accumulator then takes at most 5 x 12 = 60 steps,
+// against the 36 of a fold unit.
+template <bool CROSS, bool DIRECT>
+__global__ void __launch_bounds__(kernel_threads(DIRECT), 1) allpairs_tc_kernel(const __grid_constant__ CUtensorMap map_hi_a,
                                                                   const __grid_constant__ CUtensorMap map_lo_a,
                                                                   const __grid_constant__ CUtensorMap map_hi_b,
                                                                   const __grid_constant__ CUtensorMap map_lo_b,
@@ -229,9 +245,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) allpairs_tc_kernel(const __grid_c
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + SMEM_BAR);
   uint64_t* full = bars;                  // [NSTAGE] operands landed
   uint64_t* empty = bars + NSTAGE;        // [NSTAGE] operands consumed by the MMAs
-  uint64_t* pfull = bars + 2 * NSTAGE;    // P holds a finished fold unit
-  uint64_t* pempty = pfull + 1;           // P folded by all worker warps
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(pempty + 1);
+  uint64_t* pfull = bars + 2 * NSTAGE;    // [2] P holds a finished fold unit (DIRECT: buffer b holds a tile)
+  uint64_t* pempty = pfull + 2;           // [2] P folded by all worker warps (DIRECT: buffer b read)
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(pempty + 2);
   volatile int* fail_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
   CrossCol* colv = reinterpret_cast<CrossCol*>(smem + SMEM_COLV);
 
@@ -243,8 +259,10 @@ __global__ void __launch_bounds__(NTHREADS, 1) allpairs_tc_kernel(const __grid_c
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    mbar_init(pfull, 1);
-    mbar_init(pempty, NEPI);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&pfull[b], 1);
+      mbar_init(&pempty[b], NEPI);
+    }
     *fail_flag = 0;
     fence_mbar_init();
   }
@@ -291,7 +309,44 @@ __global__ void __launch_bounds__(NTHREADS, 1) allpairs_tc_kernel(const __grid_c
     }
   } else if (warp == 1) {
     // ---------------- MMA issuer ----------------
-    if (lane == 0) {
+    if (lane == 0 && DIRECT) {
+      constexpr uint32_t idesc = make_idesc(TILE_M, TILE_N);
+      uint32_t it = 0, k = 0;  // k blocks issued, tiles committed
+      bool ok = true;
+      for (int64_t t = blockIdx.x; t < n_tiles && ok; t += gridDim.x) {
+        const uint32_t buf = k & 1;
+        if (k >= 2 && (!wait_bar(&pempty[buf], ((k - 2) >> 1) & 1, args.err) || *fail_flag)) {
+          *fail_flag = 1;
+          ok = false;
+          break;
+        }
+        const uint32_t d_tmem = tmem_base + (buf ? R_COL : P_COL);
+        for (int kb = 0; kb < nkb; ++kb, ++it) {
+          const int s = it % NSTAGE;
+          if (!wait_bar(&full[s], (it / NSTAGE) & 1, args.err)) {
+            *fail_flag = 1;
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t st = smem_addr(smem + s * STAGE_BYTES);
+          const uint32_t a_hi = st, a_lo = st + A_BYTES, b_hi = st + 2 * A_BYTES, b_lo = st + 2 * A_BYTES + B_BYTES;
+#pragma unroll
+          for (int ks = 0; ks < KBLK / 16; ++ks) {
+            const uint32_t koff = ks * 32;
+            tc_mma(d_tmem, smem_desc_sw128(a_hi + koff), smem_desc_sw128(b_hi + koff), idesc,
+                   (kb == 0 && ks == 0) ? 0u : 1u);
+            tc_mma(d_tmem, smem_desc_sw128(a_hi + koff), smem_desc_sw128(b_lo + koff), idesc, 1u);
+            tc_mma(d_tmem, smem_desc_sw128(a_lo + koff), smem_desc_sw128(b_hi + koff), idesc, 1u);
+          }
+          tc_commit(&empty[s]);
+        }
+        if (!ok) break;
+        tc_commit(&pfull[buf]);  // the tile is complete in buffer buf
+        ++k;
+      }
+      if (k > 0) wait_bar(&pfull[(k - 1) & 1], ((k - 1) >> 1) & 1, args.err);  // no MMA left in flight
+    } else if (lane == 0) {
       constexpr uint32_t idesc = make_idesc(TILE_M, TILE_N);
       const uint32_t d_tmem = tmem_base + P_COL;
       uint32_t it = 0, unit = 0;  // k blocks issued, fold units committed
@@ -336,7 +391,11 @@ __global__ void __launch_bounds__(NTHREADS, 1) allpairs_tc_kernel(const __grid_c
     const int slice = warp & 3;           // TMEM lanes [32*slice, 32*slice + 32)
     const int grp = ew >> 2;              // column group: columns [80*grp, 80*grp + 80)
     const int row = slice * 32 + lane;    // accumulator row of this thread
-    const int etid = ew * 32 + lane;      // 0 .. NEPI_THREADS-1
+    const int etid = ew * 32 + lane;      // 0 .. worker threads - 1
+    constexpr int WT = DIRECT ? NEPI_D_THREADS : NEPI_THREADS;  // worker threads
+    constexpr int ppc = DIRECT ? 1 : PASSES_PER_CHUNK;          // passes per chunk
+    constexpr int passes = NCHUNK * ppc;                         // per tile
+    const bool stager = ew < NEPI;        // the warps that read tensor memory
     const float inv_n = 1.0f / (float)args.A;
     const uint32_t lane_off = (uint32_t)(slice * 32) << 16;
     bool pend = false;   // a tile waits in R for its epilogue
@@ -344,21 +403,27 @@ __global__ void __launch_bounds__(NTHREADS, 1) allpairs_tc_kernel(const __grid_c
     int64_t pi0 = 0, pj0 = 0;
 
     // One epilogue pass of the pending tile: the first pass of a chunk stages
-    // the chunk from R (one 16-column TMEM load per warp), then every thread
-    // takes at most one of the chunk's frame pairs.
-    auto do_pass = [&]() {
-      const int ch = pass / PASSES_PER_CHUNK, sub = pass % PASSES_PER_CHUNK;
+    // the 48-column chunk from tensor memory (column `tcol`) into shared
+    // memory by one 16-column load per staging warp, then every thread takes
+    // at most one of the chunk's 672 frame pairs.  `after_stage` runs once
+    // the warp's tensor-memory read is complete (DIRECT: the release of the
+    // buffer after the last chunk).
+    auto do_pass = [&](uint32_t tcol, auto&& after_stage) {
+      const int ch = pass / ppc, sub = pass % ppc;
       if (sub == 0) {
         if (CROSS && ch == 0 && etid < FR_N) colv[etid] = cross_col(args.reqs, args.colreq, pj0 + etid, args.n_b);
-        float v[16];
-        tc_ld16(tmem_base + R_COL + (uint32_t)(ch * EPI_COLS + grp * 16) + lane_off, v);
-        tc_wait_ld();
-        float* dst = sD + row * EPI_LD + grp * 16;
+        if (stager) {
+          float v[16];
+          tc_ld16(tmem_base + tcol + (uint32_t)(ch * EPI_COLS + grp * 16) + lane_off, v);
+          tc_wait_ld();
+          float* dst = sD + row * EPI_LD + grp * 16;
 #pragma unroll
-        for (int q = 0; q < 16; ++q) dst[q] = v[q];
-        named_bar(1, NEPI_THREADS);
+          for (int q = 0; q < 16; ++q) dst[q] = v[q];
+          after_stage(ch);
+        }
+        named_bar(1, WT);
       }
-      const int p = sub * NEPI_THREADS + etid;
+      const int p = sub * WT + etid;
       if (p < CHUNK_PAIRS) {
         if (CROSS) {
           // consecutive threads take consecutive row frames of one column frame:
@@ -389,18 +454,45 @@ __global__ void __launch_bounds__(NTHREADS, 1) allpairs_tc_kernel(const __grid_c
           }
         }
       }
-      if (sub == PASSES_PER_CHUNK - 1) {
+      if (sub == ppc - 1) {
         tc_fence_before();
-        named_bar(1, NEPI_THREADS);  // chunk (and, after the last, R) no longer read
+        named_bar(1, WT);  // chunk (and, after the last, R) no longer read
         tc_fence_after();
       }
-      if (++pass == PASSES) pend = false;
+      if (++pass == passes) pend = false;
     };
+    auto nothing = [](int) {};
 
     uint32_t unit = 0;
     bool failed = false;
-    const int ppu = (PASSES + nunit - 1) / nunit;  // epilogue passes after each fold
-    for (int64_t t = blockIdx.x; t < n_tiles && !failed; t += gridDim.x) {
+    if (DIRECT) {
+      uint32_t k = 0;
+      for (int64_t t = blockIdx.x; t < n_tiles && !failed; t += gridDim.x, ++k) {
+        const uint32_t buf = k & 1;
+        const bool ok = __all_sync(FULL_MASK, wait_bar(&pfull[buf], (k >> 1) & 1, args.err) && !*fail_flag);
+        if (named_bar_or(2, WT, !ok)) {  // one answer for all worker warps
+          failed = true;
+          break;
+        }
+        tc_fence_after();
+        const int2 tl = args.tiles[t];
+        pi0 = (int64_t)tl.x * FR_M;
+        pj0 = (int64_t)tl.y * FR_N;
+        pend = true;
+        pass = 0;
+        auto release = [&](int ch) {
+          if (ch == NCHUNK - 1) {  // this warp's last read of the buffer
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&pempty[buf]);
+          }
+        };
+        while (pend) do_pass(buf ? R_COL : P_COL, release);
+      }
+      if (failed) *fail_flag = 1;
+    }
+    const int ppu = (passes + nunit - 1) / nunit;  // epilogue passes after each fold
+    for (int64_t t = blockIdx.x; !DIRECT && t < n_tiles && !failed; t += gridDim.x) {
       float acc[GCOLS];
 #pragma unroll
       for (int q = 0; q < GCOLS; ++q) acc[q] = 0.f;
@@ -423,10 +515,10 @@ __global__ void __launch_bounds__(NTHREADS, 1) allpairs_tc_kernel(const __grid_c
         tc_fence_before();
         __syncwarp();
         if (lane == 0) mbar_arrive(pempty);
-        for (int r = 0; r < ppu && pend; ++r) do_pass();
+        for (int r = 0; r < ppu && pend; ++r) do_pass(R_COL, nothing);
       }
       if (failed) break;
-      while (pend) do_pass();  // R must be free before this tile goes in
+      while (pend) do_pass(R_COL, nothing);  // R must be free before this tile goes in
       {
         const uint32_t taddr = tmem_base + R_COL + (uint32_t)(grp * GCOLS) + lane_off;
 #pragma unroll
@@ -447,9 +539,11 @@ __global__ void __launch_bounds__(NTHREADS, 1) allpairs_tc_kernel(const __grid_c
       pend = true;
       pass = 0;
     }
-    if (failed) *fail_flag = 1;
-    else
-      while (pend) do_pass();
+    if (!DIRECT) {
+      if (failed) *fail_flag = 1;
+      else
+        while (pend) do_pass(R_COL, nothing);
+    }
   }
 
   tc_fence_before();
@@ -545,10 +639,18 @@ int launch_allpairs_tc(const __nv_bfloat16* Xhi, const __nv_bfloat16* Xlo, const
   a.reqs = nullptr;
   a.colreq = nullptr;
   a.n_b = 0;
-  GB_CUDA_TRY(cudaFuncSetAttribute(allpairs_tc_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_TOTAL),
-              "cudaFuncSetAttribute(allpairs_tc_kernel)");
   const int64_t grid = a.n_tiles < sm_count() ? a.n_tiles : sm_count();
-  allpairs_tc_kernel<false><<<(unsigned)grid, NTHREADS, SMEM_TOTAL, st>>>(mha, mla, mhb, mlb, a);
+  if (kpad / KBLK <= DIRECT_MAX_KB) {
+    GB_CUDA_TRY(cudaFuncSetAttribute(allpairs_tc_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     SMEM_TOTAL),
+                "cudaFuncSetAttribute(allpairs_tc_kernel)");
+    allpairs_tc_kernel<false, true><<<(unsigned)grid, NTHREADS_D, SMEM_TOTAL, st>>>(mha, mla, mhb, mlb, a);
+  } else {
+    GB_CUDA_TRY(cudaFuncSetAttribute(allpairs_tc_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     SMEM_TOTAL),
+                "cudaFuncSetAttribute(allpairs_tc_kernel)");
+    allpairs_tc_kernel<false, false><<<(unsigned)grid, NTHREADS, SMEM_TOTAL, st>>>(mha, mla, mhb, mlb, a);
+  }
   GB_CUDA_TRY(cudaGetLastError(), "launch allpairs_tc_kernel");
   // (a pageable host->device cudaMemcpyAsync returns once the source has been
   // staged, so the host tile list may go out of scope here)
@@ -591,10 +693,18 @@ int launch_cross_tc(const __nv_bfloat16* Ahi, const __nv_bfloat16* Alo, const do
   a.reqs = reqs;
   a.colreq = colreq;
   a.n_b = cap_b;
-  GB_CUDA_TRY(cudaFuncSetAttribute(allpairs_tc_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_TOTAL),
-              "cudaFuncSetAttribute(cross_tc_kernel)");
   const int64_t grid = n_tiles < sm_count() ? n_tiles : sm_count();
-  allpairs_tc_kernel<true><<<(unsigned)grid, NTHREADS, SMEM_TOTAL, st>>>(mha, mla, mhb, mlb, a);
+  if (kpad / KBLK <= DIRECT_MAX_KB) {
+    GB_CUDA_TRY(cudaFuncSetAttribute(allpairs_tc_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     SMEM_TOTAL),
+                "cudaFuncSetAttribute(cross_tc_kernel)");
+    allpairs_tc_kernel<true, true><<<(unsigned)grid, NTHREADS_D, SMEM_TOTAL, st>>>(mha, mla, mhb, mlb, a);
+  } else {
+    GB_CUDA_TRY(cudaFuncSetAttribute(allpairs_tc_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     SMEM_TOTAL),
+                "cudaFuncSetAttribute(cross_tc_kernel)");
+    allpairs_tc_kernel<true, false><<<(unsigned)grid, NTHREADS, SMEM_TOTAL, st>>>(mha, mla, mhb, mlb, a);
+  }
   GB_CUDA_TRY(cudaGetLastError(), "launch cross_tc_kernel");
   return GBRMSD_OK;
 }
