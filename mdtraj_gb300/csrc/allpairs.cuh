@@ -239,14 +239,14 @@ __device__ __forceinline__ bool pair_needs_refine(float r, float ga, float gb, f
 // of M (split-BF16 or FP32 accumulation) is ~1e-6 * scale / sqrt(n) in msd
 // units, i.e. <= 2e-5 nm in rmsd above r = 0.25 * scale / sqrt(n) (scale =
 // (Ga + Gb) / 2n in nm^2); below it the pair is recomputed.
-__device__ __forceinline__ void pair_epilogue(int64_t i, int64_t j, const float (&m)[9], const double* __restrict__ G,
-                                              float inv_n, int64_t F, float* __restrict__ out, PairRefine* rl,
-                                              int* rc, int rcap, int* err) {
+// (ga, gb: the two frames' traces rounded to float.)
+__device__ __forceinline__ void pair_epilogue_g(int64_t i, int64_t j, const float (&m)[9], float ga, float gb,
+                                                float inv_n, int64_t F, float* __restrict__ out, PairRefine* rl,
+                                                int* rc, int rcap, int* err) {
   if (i == j) {
     out[i * F + i] = 0.f;
     return;
   }
-  const float ga = (float)G[i], gb = (float)G[j];
   bool unresolved;
   const float msd = qcp_msd_f32(m, ga, gb, inv_n, unresolved);
   const float r = sqrtf(msd);
@@ -259,6 +259,12 @@ __device__ __forceinline__ void pair_epilogue(int64_t i, int64_t j, const float 
     else
       atomicOr(err, DEV_ERR_REFINE_OVERFLOW);
   }
+}
+
+__device__ __forceinline__ void pair_epilogue(int64_t i, int64_t j, const float (&m)[9], const double* __restrict__ G,
+                                              float inv_n, int64_t F, float* __restrict__ out, PairRefine* rl,
+                                              int* rc, int rcap, int* err) {
+  pair_epilogue_g(i, j, m, (float)G[i], (float)G[j], inv_n, F, out, rl, rc, rcap, err);
 }
 
 // Cross RMSD (query set against a database): the output row and database

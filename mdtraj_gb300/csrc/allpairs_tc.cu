@@ -95,7 +95,8 @@ constexpr int SMEM_STAGES = NSTAGE * STAGE_BYTES;
 constexpr int SMEM_EPI = SMEM_STAGES;
 constexpr int SMEM_BAR = SMEM_EPI + ((EPI_BYTES + 127) / 128) * 128;
 constexpr int SMEM_COLV = SMEM_BAR + 128;
-constexpr int SMEM_TOTAL = SMEM_COLV + FR_N * (int)sizeof(CrossCol) + 1024;  // + slack for 1024-byte alignment
+constexpr int SMEM_G = SMEM_COLV + FR_N * (int)sizeof(CrossCol);  // traces of the tile's frames as float
+constexpr int SMEM_TOTAL = SMEM_G + (FR_M + FR_N) * 4 + 1024;        // + slack for 1024-byte alignment
 
 struct TcArgs {
   const double* G;    // traces of the row frames
@@ -250,6 +251,8 @@ __global__ void __launch_bounds__(kernel_threads(DIRECT), 1) allpairs_tc_kernel(
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(pempty + 2);
   volatile int* fail_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
   CrossCol* colv = reinterpret_cast<CrossCol*>(smem + SMEM_COLV);
+  float* sGa = reinterpret_cast<float*>(smem + SMEM_G);  // [FR_M] row frames of the pending tile
+  float* sGb = sGa + FR_M;                               // [FR_N] column frames
 
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
@@ -411,7 +414,16 @@ __global__ void __launch_bounds__(kernel_threads(DIRECT), 1) allpairs_tc_kernel(
     auto do_pass = [&](uint32_t tcol, auto&& after_stage) {
       const int ch = pass / ppc, sub = pass % ppc;
       if (sub == 0) {
-        if (CROSS && ch == 0 && etid < FR_N) colv[etid] = cross_col(args.reqs, args.colreq, pj0 + etid, args.n_b);
+        if (ch == 0) {
+          // per tile: the request of each column frame, and the frames'
+          // traces rounded to float once (not per pair on the FP64 pipe)
+          if (CROSS && etid < FR_N) colv[etid] = cross_col(args.reqs, args.colreq, pj0 + etid, args.n_b);
+          if (etid < FR_M) sGa[etid] = pi0 + etid < args.F ? (float)args.G[pi0 + etid] : 0.f;
+          if (etid < FR_N) {
+            const int64_t j = pj0 + etid;
+            sGb[etid] = CROSS ? (j < args.n_b ? (float)args.Gb[j] : 0.f) : (j < args.F ? (float)args.G[j] : 0.f);
+          }
+        }
         if (stager) {
           float v[16];
           tc_ld16(tmem_base + tcol + (uint32_t)(ch * EPI_COLS + grp * 16) + lane_off, v);
@@ -438,8 +450,8 @@ __global__ void __launch_bounds__(kernel_threads(DIRECT), 1) allpairs_tc_kernel(
 #pragma unroll
               for (int d = 0; d < 3; ++d) m[3 * c + d] = sD[(3 * li + c) * EPI_LD + 3 * lj + d];
             const int64_t j = pj0 + ch * 16 + lj;
-            cross_pair(i, j, m, (float)args.G[i], (float)args.Gb[j], inv_n, cv.row + (i - cv.db0), args.rl,
-                       args.rc, args.rcap, args.err);
+            cross_pair(i, j, m, sGa[li], sGb[ch * 16 + lj], inv_n, cv.row + (i - cv.db0), args.rl, args.rc,
+                       args.rcap, args.err);
           }
         } else {
           const int li = p >> 4, lj = p & 15;
@@ -450,7 +462,8 @@ __global__ void __launch_bounds__(kernel_threads(DIRECT), 1) allpairs_tc_kernel(
             for (int c = 0; c < 3; ++c)
 #pragma unroll
               for (int d = 0; d < 3; ++d) m[3 * c + d] = sD[(3 * li + c) * EPI_LD + 3 * lj + d];
-            pair_epilogue(i, j, m, args.G, inv_n, args.F, args.out, args.rl, args.rc, args.rcap, args.err);
+            pair_epilogue_g(i, j, m, sGa[li], sGb[ch * 16 + lj], inv_n, args.F, args.out, args.rl, args.rc,
+                            args.rcap, args.err);
           }
         }
       }
