@@ -1057,6 +1057,18 @@ def run_serving(args) -> dict:
                                 host_pool_bytes=4 << 30)
     base = serving.RmsdServer(dbs, method="fp32", query_capacity=1024, hbm_budget_bytes=48 << 30, slots=1,
                               max_batch_requests=1)
+    # the rate of the result copies into the page-locked host result pool on this machine, now
+    probe = torch.ones(256 << 20, dtype=torch.uint8, device=dev)
+    from mdtraj_gb300 import _device as Dv
+    s_probe = torch.cuda.current_stream().cuda_stream
+    Dv.copy_rows(server.hpool.ptr(0), probe.numel(), probe.data_ptr(), probe.numel(), probe.numel(), 1, 2, s_probe)
+    torch.cuda.synchronize()
+    t_probe = time.perf_counter()
+    for _ in range(4):
+        Dv.copy_rows(server.hpool.ptr(0), probe.numel(), probe.data_ptr(), probe.numel(), probe.numel(), 1, 2, s_probe)
+    torch.cuda.synchronize()
+    pool_gbs = 4 * probe.numel() / (time.perf_counter() - t_probe) / 1e9
+    del probe
     warm = serving_requests(host_frames, frame_ids, 24, 1e6, 1, max_q, slice_range, F)
     server.serve(warm, realtime=False, keep_results=False)
     base.serve(serving_requests(host_frames, frame_ids, 4, 1e6, 2, max_q, slice_range, F), realtime=False,
@@ -1067,9 +1079,15 @@ def run_serving(args) -> dict:
             n = max(20, min(int(rate * args.serve_seconds), args.serve_max))
             reqs = serving_requests(host_frames, frame_ids, n, rate, 1000 + k, max_q, slice_range, F)
             b0 = server.n_batches
+            l0 = len(server.batch_log)
+            t_serve = time.perf_counter()
             done = server.serve(reqs, realtime=True, keep_results=False)
+            t_serve = time.perf_counter() - t_serve
             row = {"offered_rate": rate, "requests": n, "continuous": serving.latency_summary(done)}
             row["continuous"]["mean_batch_requests"] = round(n / max(1, server.n_batches - b0), 2)
+            # where the time went: the batches' GPU time against the loop's wall time
+            row["continuous"]["batches"] = serving.batch_summary(server.batch_log[l0:])
+            row["continuous"]["batches"]["wall_s"] = round(t_serve, 3)
             nb = min(n, args.baseline_max)
             reqs_b = [serving.Request(queries=r.queries, db0=r.db0, db1=r.db1, arrival=r.arrival, rid=r.rid)
                       for r in reqs[:nb]]
@@ -1152,6 +1170,7 @@ def run_serving(args) -> dict:
                    "latency": "arrival to results in pinned host memory",
                    "host_result_pool_gb": round(server.hpool.buf.nbytes / 1e9, 1),
                    "host_result_pool_locked": bool(server.hpool.locked),
+                   "host_result_pool_copy_gbs": round(pool_gbs, 1),
                    "l2": "database (%.1f GB prepared) larger than L2; no flush" % (dbs.buf.numel() / 1e9)},
         "sweep": sweep,
         "speedup_at_top_rate": round(top["continuous"]["queries_per_s"] /

@@ -34,6 +34,7 @@ struct RaggedSeg {
   int64_t frame0;   // first global frame (output index)
   int64_t ref_off;  // byte offset of the segment's prepared reference in the workspace
   int32_t n_atoms, n_padded, splits, n_frames;
+  double inv_atoms;  // 1 / n_atoms
 };
 
 struct RaggedArgs {
@@ -403,6 +404,7 @@ __global__ void __launch_bounds__(256) ragged_finish_kernel(const RaggedFinishAr
   c.recs = a.sums + (sg.unit0 + f * sg.splits) * SUMS_STRIDE;
   c.S = sg.splits;
   c.A = sg.n_atoms;
+  c.inv_a = sg.inv_atoms;
   c.mode = MODE_CENTER;
   c.ref_info = reinterpret_cast<const RefInfo*>(r);
   c.ref_prefix = reinterpret_cast<const double*>(r + ref_prefix_off(sg.n_padded));
@@ -535,6 +537,7 @@ int build_tables(const int64_t* x_off, const int32_t* atoms, const int32_t* padd
     RaggedSeg& g = t.segs[s];
     g.x_off = x_off[s];
     g.n_atoms = atoms[s];
+    g.inv_atoms = 1.0 / (double)atoms[s];
     g.n_padded = padded[s];
     g.n_frames = (int32_t)frames[s];
     const int32_t Q = (atoms[s] + 3) / 4;

@@ -353,6 +353,7 @@ __global__ void __launch_bounds__(256) finish_kernel(const FinishArgs a) {
   c.recs = a.sums + f * (int64_t)a.splits * SUMS_STRIDE;
   c.S = a.splits;
   c.A = a.n_atoms;
+  c.inv_a = a.inv_atoms;
   c.mode = a.mode;
   c.ref_info = a.ref_info;
   c.ref_prefix = a.ref_prefix;
@@ -927,6 +928,7 @@ int gbrmsd_rmsd_to_reference(const float* x, int64_t n_frames, int32_t n_atoms, 
   FinishArgs fa;
   fa.n_frames = n_frames;
   fa.n_atoms = n_atoms;
+  fa.inv_atoms = 1.0 / (double)n_atoms;
   fa.splits = S;
   fa.sums = sa.sums;
   fa.ref_info = reinterpret_cast<const RefInfo*>(rw + RL.info_off);
@@ -1009,6 +1011,7 @@ int gbrmsd_rotations(const float* x, int64_t n_frames, int32_t n_atoms, int32_t 
   FinishArgs fa{};
   fa.n_frames = n_frames;
   fa.n_atoms = n_atoms;
+  fa.inv_atoms = 1.0 / (double)n_atoms;
   fa.splits = S;
   fa.sums = sa.sums;
   fa.ref_info = reinterpret_cast<const RefInfo*>(rw + RL.info_off);
@@ -1118,6 +1121,7 @@ int gbrmsd_center_inplace(float* x, int64_t n_frames, int32_t n_atoms, int32_t n
   FinishArgs fa{};
   fa.n_frames = n_frames;
   fa.n_atoms = n_atoms;
+  fa.inv_atoms = 1.0 / (double)n_atoms;
   fa.splits = S;
   fa.sums = sa.sums;
   fa.out_centroid = cent;

@@ -61,6 +61,7 @@ int64_t skip_unit_hook();
 struct FinishArgs {
   int64_t n_frames;
   int32_t n_atoms;
+  double inv_atoms;           // 1 / n_atoms
   int32_t splits;
   const double* sums;
   const RefInfo* ref_info;

@@ -231,6 +231,7 @@ __device__ __forceinline__ void accum_quad(float (&acc)[NV], const float (&ax)[4
 struct FrameCtx {
   const double* recs;      // S records of SUMS_STRIDE doubles
   int32_t S, A, mode;
+  double inv_a;            // 1 / A, computed once by the caller (FP64 division is slow on GB300)
   const RefInfo* ref_info;
   const double* ref_prefix;
   float g_target;          // MODE_PRECENTERED: supplied trace of this frame
@@ -249,7 +250,7 @@ __device__ __forceinline__ void finish_frame(const FrameCtx& c, float* out_rmsd,
   const int32_t Q = (A + 3) >> 2;
   const double* base = c.recs;
   const double dA = (double)A;
-  const double invA = 1.0 / dA;  // the frame's one FP64 division (a narrow pipe on GB300)
+  const double invA = c.inv_a;  // no FP64 division per frame: GB300's FP64 pipe is narrow
   const int64_t f = c.out_idx;
 
   if (c.mode == MODE_NOSUPERPOSE) {

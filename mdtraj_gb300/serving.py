@@ -204,6 +204,8 @@ class QueryStaging:
 
 
 class _Slot:
+    timeline = None
+
     def __init__(self, device):
         self.stream = torch.cuda.Stream(device=device)
         self.ws = CrossWorkspace(device)
@@ -252,6 +254,7 @@ class RmsdServer:
         self.hpool = HostResultPool(host_pool_bytes) if result_to_host else None
         self.n_batches = 0
         self.batch_sizes = []
+        self.batch_log = []  # per completed batch: requests, result bytes, host launch time, GPU kernels / copies
 
     # -- request checks ---------------------------------------------------
     def validate(self, r: Request) -> None:
@@ -310,9 +313,13 @@ class RmsdServer:
             p += r.n_query
 
     def _launch(self, slot: _Slot, batch: list, now: float) -> None:
+        t_host = time.perf_counter()
         self._group_by_range(batch)
         s = slot.stream
+        # per-batch timeline on the slot's stream: start, kernels done, copies done
+        t_ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
         with torch.cuda.stream(s):
+            t_ev[0].record(s)
             for r in batch:
                 rows = self.staging[r._p0:r._p0 + r.n_query]
                 q = r.queries.reshape(r.n_query, -1)
@@ -329,6 +336,7 @@ class RmsdServer:
             ws = slot.ws.get(self.n_db, self.qcap, len(batch))
             cross_launch(self.db, self.n_db, self.qset, table, len(batch), self.method, ws, s.cuda_stream)
             slot.hdr.copy_(ws[:8].view(torch.int32), non_blocking=True)
+            t_ev[1].record(s)
             if self.result_to_host:
                 for r in batch:
                     nb = 4 * r._out.numel()
@@ -337,14 +345,14 @@ class RmsdServer:
                     else:
                         r._host = torch.empty(r._out.numel(), dtype=torch.float32, pin_memory=True)
                         r._host.copy_(r._out, non_blocking=True)
-            ev = torch.cuda.Event()
-            ev.record(s)
+            t_ev[2].record(s)
         for r in batch:
             r.t_launch = now
             r.batch = self.n_batches
         self.n_batches += 1
         self.batch_sizes.append(len(batch))
-        slot.event, slot.batch, slot.ws_buf = ev, batch, ws
+        slot.event, slot.batch, slot.ws_buf = t_ev[2], batch, ws
+        slot.timeline = (t_ev, time.perf_counter() - t_host, sum(r.result_bytes for r in batch))
 
     def _unadmit(self, r: Request) -> None:
         """Returns an admitted, not launched request's pool rows, budget and
@@ -369,6 +377,10 @@ class RmsdServer:
             raise _lib.GbrmsdError(_lib.E_DEVICE, "cross RMSD batch: device error word 0x%x (1 = wait expired, "
                                                   "4 = refinement list full)" % err)
         done = slot.batch
+        t_ev, host_s, nbytes = slot.timeline
+        self.batch_log.append({"requests": len(done), "result_bytes": nbytes, "launch_host_ms": host_s * 1e3,
+                               "kernels_ms": t_ev[0].elapsed_time(t_ev[1]),
+                               "copies_ms": t_ev[1].elapsed_time(t_ev[2])})
         for r in done:
             shape = (r.n_query, r.db1 - r.db0)
             # a request withdrawn or out of time while its batch ran: the
@@ -495,3 +507,20 @@ def latency_summary(done: list, t_first: float | None = None) -> dict:
             "queries_per_s": round(len(done) / max(t1 - t0, 1e-9), 1),
             "query_frames_per_s": round(sum(r.n_query for r in done) / max(t1 - t0, 1e-9), 1),
             "pairs_per_s": round(sum(r.n_query * (r.db1 - r.db0) for r in done) / max(t1 - t0, 1e-9), 1)}
+
+
+def batch_summary(log: list) -> dict:
+    """Where a serving run's batches spent their time: mean requests per
+    batch, host time to launch one, GPU time of its kernels (query upload,
+    preparation, cross RMSD) and of its result copies to host memory, and the
+    copies' rate."""
+    if not log:
+        return {"batches": 0}
+    k = np.array([b["kernels_ms"] for b in log])
+    c = np.array([b["copies_ms"] for b in log])
+    nb = float(sum(b["result_bytes"] for b in log))
+    return {"batches": len(log), "mean_requests": round(float(np.mean([b["requests"] for b in log])), 2),
+            "launch_host_ms": round(float(np.mean([b["launch_host_ms"] for b in log])), 3),
+            "kernels_ms": round(float(k.mean()), 3), "copies_ms": round(float(c.mean()), 3),
+            "copies_gbs": round(nb / max(c.sum() / 1e3, 1e-9) / 1e9, 1),
+            "gpu_ms_total": round(float(k.sum() + c.sum()), 1)}
