@@ -34,6 +34,15 @@
 // Every wait is bounded; the workers agree on a failure at every fold unit
 // (barrier with an OR reduction) so that no named barrier can be left half
 // entered; the CTA frees its tensor memory before exiting.
+//
+// Frames of at most 320 atoms (5 k blocks) use the DIRECT variant, 864
+// threads: the MMAs of a tile accumulate all its k blocks in one of two
+// tensor-memory buffers (no fold), alternating by tile; warps 2-5 stage the
+// finished buffer into shared memory chunk by chunk, and warps 6-26 solve one
+// frame pair each per chunk.  Stagers and solvers hand over through two
+// mbarriers (chunk staged / chunk read by every solver), so a solver copies
+// its 3x3 block to registers and goes on, and only the staging of the chunk
+// after next waits for it.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <string.h>
@@ -74,17 +83,20 @@ constexpr int NEPI = 4 * NGROUP;        // worker warps
 constexpr int NEPI_THREADS = 32 * NEPI;
 constexpr int NTHREADS = 64 + NEPI_THREADS;
 constexpr int PASSES_PER_CHUNK = (CHUNK_PAIRS + NEPI_THREADS - 1) / NEPI_THREADS;  // 2
-constexpr int PASSES = NCHUNK * PASSES_PER_CHUNK;                                 // 10 per tile
 // DIRECT kernel (frames of at most DIRECT_MAX_KB k blocks, 320 atoms): no
-// accumulators in registers, so a worker needs ~72 of them and 21 worker
-// warps fit -- one thread per frame pair of a chunk (one pass per chunk, 5
-// per tile) and ~5 warps per scheduler to hide the epilogue's dependent FP32
-// chains; the first NEPI of them stage the chunks from tensor memory.
+// accumulators in registers, so a thread needs ~72 of them and 25 epilogue
+// warps fit: 4 stagers (one per tensor-memory lane slice: three 16-column
+// loads each per chunk) and 21 solvers, one thread per frame pair of a
+// chunk, ~6 warps per scheduler to hide the epilogue's dependent FP32 chains.
+// Stagers and solvers hand chunks over through two mbarriers (chunk staged;
+// chunk read), so a solver that has copied its 3x3 block into registers
+// never waits for a slower solver's QCP before the next chunk is staged.
 constexpr int DIRECT_MAX_KB = 5;
-constexpr int NEPI_D = (CHUNK_PAIRS + 31) / 32;          // 21
+constexpr int NSTAGER_D = 4;
+constexpr int NEPI_D = (CHUNK_PAIRS + 31) / 32;          // 21 solver warps
 constexpr int NEPI_D_THREADS = 32 * NEPI_D;             // 672
-constexpr int NTHREADS_D = 64 + NEPI_D_THREADS;          // 736
-static_assert(NEPI_D_THREADS >= CHUNK_PAIRS && NEPI_D >= NEPI, "one pair per thread per chunk");
+constexpr int NTHREADS_D = 64 + 32 * NSTAGER_D + NEPI_D_THREADS;  // 864
+static_assert(NEPI_D_THREADS >= CHUNK_PAIRS, "one pair per solver thread per chunk");
 __host__ __device__ constexpr int kernel_threads(bool direct) { return direct ? NTHREADS_D : NTHREADS; }
 constexpr uint32_t SPIN = 1u << 24;
 static_assert(EPI_COLS == NGROUP * 16, "one 16-column TMEM load per worker warp per chunk");
@@ -248,7 +260,9 @@ __global__ void __launch_bounds__(kernel_threads(DIRECT), 1) allpairs_tc_kernel(
   uint64_t* empty = bars + NSTAGE;        // [NSTAGE] operands consumed by the MMAs
   uint64_t* pfull = bars + 2 * NSTAGE;    // [2] P holds a finished fold unit (DIRECT: buffer b holds a tile)
   uint64_t* pempty = pfull + 2;           // [2] P folded by all worker warps (DIRECT: buffer b read)
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(pempty + 2);
+  uint64_t* sfull = pempty + 2;           // DIRECT: a chunk is staged in shared memory
+  uint64_t* sfree = sfull + 1;            // DIRECT: every solver has read the staged chunk
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sfree + 1);
   volatile int* fail_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
   CrossCol* colv = reinterpret_cast<CrossCol*>(smem + SMEM_COLV);
   float* sGa = reinterpret_cast<float*>(smem + SMEM_G);  // [FR_M] row frames of the pending tile
@@ -264,8 +278,10 @@ __global__ void __launch_bounds__(kernel_threads(DIRECT), 1) allpairs_tc_kernel(
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&pfull[b], 1);
-      mbar_init(&pempty[b], NEPI);
+      mbar_init(&pempty[b], DIRECT ? NSTAGER_D : NEPI);
     }
+    mbar_init(sfull, 32 * NSTAGER_D);
+    mbar_init(sfree, NEPI_D_THREADS);
     *fail_flag = 0;
     fence_mbar_init();
   }
@@ -389,16 +405,109 @@ __global__ void __launch_bounds__(kernel_threads(DIRECT), 1) allpairs_tc_kernel(
       if (unit > 0) wait_bar(pfull, (unit - 1) & 1, args.err);  // no MMA left in flight
     }
   } else {
+    // ---------------- DIRECT: stager and solver warps ----------------
+    if constexpr (DIRECT) {
+      const float inv_n = 1.0f / (float)args.A;
+      bool failed = false;
+      uint32_t k = 0, g = 0;  // tiles, chunks of this CTA
+      if (warp < 2 + NSTAGER_D) {
+        // stager: tile k's buffer into shared memory, chunk by chunk
+        const int slice = warp & 3;
+        const int sid = (warp - 2) * 32 + lane;  // 0 .. 127
+        const uint32_t lane_off = (uint32_t)(slice * 32) << 16;
+        float* dst = sD + (slice * 32 + lane) * EPI_LD;
+        for (int64_t t = blockIdx.x; t < n_tiles && !failed; t += gridDim.x, ++k) {
+          const uint32_t buf = k & 1;
+          if (!wait_bar(&pfull[buf], (k >> 1) & 1, args.err) || *fail_flag) {
+            failed = true;
+            break;
+          }
+          tc_fence_after();
+          const int2 tl = args.tiles[t];
+          const int64_t pi0 = (int64_t)tl.x * FR_M, pj0 = (int64_t)tl.y * FR_N;
+          const uint32_t tcol = buf ? R_COL : P_COL;
+          for (int ch = 0; ch < NCHUNK; ++ch, ++g) {
+            if (g > 0 && (!wait_bar(sfree, (g - 1) & 1, args.err) || *fail_flag)) {
+              failed = true;
+              break;
+            }
+            if (ch == 0) {
+              // per tile: the request of each column frame, and the frames'
+              // traces rounded to float once (not per pair on the FP64 pipe)
+              if (CROSS && sid < FR_N) colv[sid] = cross_col(args.reqs, args.colreq, pj0 + sid, args.n_b);
+              if (sid < FR_M) sGa[sid] = pi0 + sid < args.F ? (float)args.G[pi0 + sid] : 0.f;
+              if (sid < FR_N) {
+                const int64_t j = pj0 + sid;
+                sGb[sid] = CROSS ? (j < args.n_b ? (float)args.Gb[j] : 0.f) : (j < args.F ? (float)args.G[j] : 0.f);
+              }
+            }
+#pragma unroll
+            for (int q = 0; q < NGROUP; ++q) {
+              float v[16];
+              tc_ld16(tmem_base + tcol + (uint32_t)(ch * EPI_COLS + q * 16) + lane_off, v);
+              tc_wait_ld();
+#pragma unroll
+              for (int c = 0; c < 16; ++c) dst[q * 16 + c] = v[c];
+            }
+            if (ch == NCHUNK - 1) {  // this warp's last read of the buffer
+              tc_fence_before();
+              __syncwarp();
+              if (lane == 0) mbar_arrive(&pempty[buf]);
+            }
+            mbar_arrive(sfull);  // every stager thread: its stores are released to the solvers
+          }
+        }
+      } else {
+        // solver: one frame pair of every chunk
+        const int p = (warp - 2 - NSTAGER_D) * 32 + lane;  // 0 .. 671
+        int li, lj;
+        if (CROSS) {
+          // consecutive threads take consecutive row frames of one column
+          // frame: contiguous in the request's output row
+          lj = p / FR_M;
+          li = p - lj * FR_M;
+        } else {
+          li = p >> 4;
+          lj = p & 15;
+        }
+        for (int64_t t = blockIdx.x; t < n_tiles && !failed; t += gridDim.x, ++k) {
+          const int2 tl = args.tiles[t];
+          const int64_t i = (int64_t)tl.x * FR_M + li;
+          for (int ch = 0; ch < NCHUNK; ++ch, ++g) {
+            if (!wait_bar(sfull, g & 1, args.err) || *fail_flag) {
+              failed = true;
+              break;
+            }
+            float m[9];
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+#pragma unroll
+              for (int d = 0; d < 3; ++d) m[3 * c + d] = sD[(3 * li + c) * EPI_LD + 3 * lj + d];
+            const float ga = sGa[li], gb = sGb[ch * 16 + lj];
+            const int64_t j = (int64_t)tl.y * FR_N + ch * 16 + lj;
+            CrossCol cv;
+            if (CROSS) cv = colv[ch * 16 + lj];
+            mbar_arrive(sfree);  // this thread's reads of the chunk are done
+            if (CROSS) {
+              if (cv.row != nullptr && i >= cv.db0 && i < cv.db1 && i < args.F)
+                cross_pair(i, j, m, ga, gb, inv_n, cv.row + (i - cv.db0), args.rl, args.rc, args.rcap, args.err);
+            } else if (i < args.F && j < args.F && i <= j) {
+              pair_epilogue_g(i, j, m, ga, gb, inv_n, args.F, args.out, args.rl, args.rc, args.rcap, args.err);
+            }
+          }
+        }
+      }
+      if (failed) *fail_flag = 1;
+    } else {
     // ---------------- worker warps (fold + interleaved epilogue) ----------------
     const int ew = warp - 2;              // 0 .. NEPI-1
     const int slice = warp & 3;           // TMEM lanes [32*slice, 32*slice + 32)
     const int grp = ew >> 2;              // column group: columns [80*grp, 80*grp + 80)
     const int row = slice * 32 + lane;    // accumulator row of this thread
     const int etid = ew * 32 + lane;      // 0 .. worker threads - 1
-    constexpr int WT = DIRECT ? NEPI_D_THREADS : NEPI_THREADS;  // worker threads
-    constexpr int ppc = DIRECT ? 1 : PASSES_PER_CHUNK;          // passes per chunk
-    constexpr int passes = NCHUNK * ppc;                         // per tile
-    const bool stager = ew < NEPI;        // the warps that read tensor memory
+    constexpr int WT = NEPI_THREADS;                 // worker threads
+    constexpr int ppc = PASSES_PER_CHUNK;            // passes per chunk
+    constexpr int passes = NCHUNK * ppc;             // per tile (10)
     const float inv_n = 1.0f / (float)args.A;
     const uint32_t lane_off = (uint32_t)(slice * 32) << 16;
     bool pend = false;   // a tile waits in R for its epilogue
@@ -406,12 +515,10 @@ __global__ void __launch_bounds__(kernel_threads(DIRECT), 1) allpairs_tc_kernel(
     int64_t pi0 = 0, pj0 = 0;
 
     // One epilogue pass of the pending tile: the first pass of a chunk stages
-    // the 48-column chunk from tensor memory (column `tcol`) into shared
-    // memory by one 16-column load per staging warp, then every thread takes
-    // at most one of the chunk's 672 frame pairs.  `after_stage` runs once
-    // the warp's tensor-memory read is complete (DIRECT: the release of the
-    // buffer after the last chunk).
-    auto do_pass = [&](uint32_t tcol, auto&& after_stage) {
+    // the 48-column chunk from R into shared memory (one 16-column load per
+    // warp), then every thread takes at most one of the chunk's 672 frame
+    // pairs.
+    auto do_pass = [&]() {
       const int ch = pass / ppc, sub = pass % ppc;
       if (sub == 0) {
         if (ch == 0) {
@@ -424,15 +531,12 @@ __global__ void __launch_bounds__(kernel_threads(DIRECT), 1) allpairs_tc_kernel(
             sGb[etid] = CROSS ? (j < args.n_b ? (float)args.Gb[j] : 0.f) : (j < args.F ? (float)args.G[j] : 0.f);
           }
         }
-        if (stager) {
-          float v[16];
-          tc_ld16(tmem_base + tcol + (uint32_t)(ch * EPI_COLS + grp * 16) + lane_off, v);
-          tc_wait_ld();
-          float* dst = sD + row * EPI_LD + grp * 16;
+        float v[16];
+        tc_ld16(tmem_base + R_COL + (uint32_t)(ch * EPI_COLS + grp * 16) + lane_off, v);
+        tc_wait_ld();
+        float* dst = sD + row * EPI_LD + grp * 16;
 #pragma unroll
-          for (int q = 0; q < 16; ++q) dst[q] = v[q];
-          after_stage(ch);
-        }
+        for (int q = 0; q < 16; ++q) dst[q] = v[q];
         named_bar(1, WT);
       }
       const int p = sub * WT + etid;
@@ -474,38 +578,11 @@ __global__ void __launch_bounds__(kernel_threads(DIRECT), 1) allpairs_tc_kernel(
       }
       if (++pass == passes) pend = false;
     };
-    auto nothing = [](int) {};
 
     uint32_t unit = 0;
     bool failed = false;
-    if (DIRECT) {
-      uint32_t k = 0;
-      for (int64_t t = blockIdx.x; t < n_tiles && !failed; t += gridDim.x, ++k) {
-        const uint32_t buf = k & 1;
-        const bool ok = __all_sync(FULL_MASK, wait_bar(&pfull[buf], (k >> 1) & 1, args.err) && !*fail_flag);
-        if (named_bar_or(2, WT, !ok)) {  // one answer for all worker warps
-          failed = true;
-          break;
-        }
-        tc_fence_after();
-        const int2 tl = args.tiles[t];
-        pi0 = (int64_t)tl.x * FR_M;
-        pj0 = (int64_t)tl.y * FR_N;
-        pend = true;
-        pass = 0;
-        auto release = [&](int ch) {
-          if (ch == NCHUNK - 1) {  // this warp's last read of the buffer
-            tc_fence_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&pempty[buf]);
-          }
-        };
-        while (pend) do_pass(buf ? R_COL : P_COL, release);
-      }
-      if (failed) *fail_flag = 1;
-    }
     const int ppu = (passes + nunit - 1) / nunit;  // epilogue passes after each fold
-    for (int64_t t = blockIdx.x; !DIRECT && t < n_tiles && !failed; t += gridDim.x) {
+    for (int64_t t = blockIdx.x; t < n_tiles && !failed; t += gridDim.x) {
       float acc[GCOLS];
 #pragma unroll
       for (int q = 0; q < GCOLS; ++q) acc[q] = 0.f;
@@ -528,10 +605,10 @@ __global__ void __launch_bounds__(kernel_threads(DIRECT), 1) allpairs_tc_kernel(
         tc_fence_before();
         __syncwarp();
         if (lane == 0) mbar_arrive(pempty);
-        for (int r = 0; r < ppu && pend; ++r) do_pass(R_COL, nothing);
+        for (int r = 0; r < ppu && pend; ++r) do_pass();
       }
       if (failed) break;
-      while (pend) do_pass(R_COL, nothing);  // R must be free before this tile goes in
+      while (pend) do_pass();  // R must be free before this tile goes in
       {
         const uint32_t taddr = tmem_base + R_COL + (uint32_t)(grp * GCOLS) + lane_off;
 #pragma unroll
@@ -552,11 +629,10 @@ __global__ void __launch_bounds__(kernel_threads(DIRECT), 1) allpairs_tc_kernel(
       pend = true;
       pass = 0;
     }
-    if (!DIRECT) {
-      if (failed) *fail_flag = 1;
-      else
-        while (pend) do_pass(R_COL, nothing);
-    }
+    if (failed) *fail_flag = 1;
+    else
+      while (pend) do_pass();
+    }  // fold kernel
   }
 
   tc_fence_before();
