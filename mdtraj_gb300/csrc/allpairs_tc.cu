@@ -98,7 +98,9 @@ constexpr int NEPI_D_THREADS = 32 * NEPI_D;             // 672
 constexpr int NTHREADS_D = 64 + 32 * NSTAGER_D + NEPI_D_THREADS;  // 864
 static_assert(NEPI_D_THREADS >= CHUNK_PAIRS, "one pair per solver thread per chunk");
 __host__ __device__ constexpr int kernel_threads(bool direct) { return direct ? NTHREADS_D : NTHREADS; }
-constexpr uint32_t SPIN = 1u << 24;
+// Limit of one pipeline wait (a k block landing, a tile finishing, a chunk
+// staged): far above any step of a healthy kernel, which takes microseconds.
+constexpr uint64_t WAIT_LIMIT_NS = 2000000000ull;
 static_assert(EPI_COLS == NGROUP * 16, "one 16-column TMEM load per worker warp per chunk");
 static_assert(R_COL + TILE_N <= TMEM_COLS && P_COL + TILE_N <= R_COL, "TMEM layout");
 
@@ -209,7 +211,7 @@ __host__ __device__ constexpr uint32_t make_idesc(int m, int n) {
 }
 
 __device__ __forceinline__ bool wait_bar(uint64_t* bar, uint32_t parity, int* err) {
-  return mbar_wait_bounded(bar, parity, err, SPIN);
+  return mbar_wait_sleep(bar, parity, err, WAIT_LIMIT_NS);
 }
 
 __device__ __forceinline__ void tc_st16(uint32_t taddr, const float (&v)[16]) {
@@ -251,9 +253,10 @@ __global__ void __launch_bounds__(kernel_threads(DIRECT), 1) allpairs_tc_kernel(
                                                                   const __grid_constant__ CUtensorMap map_hi_b,
                                                                   const __grid_constant__ CUtensorMap map_lo_b,
                                                                   const TcArgs args) {
-  extern __shared__ unsigned char smem_raw[];
-  unsigned char* smem =
-      reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  // 1024-byte aligned for the 128-byte swizzle; an offset from the shared
+  // array (not an integer cast) keeps every access below a shared-memory one
+  unsigned char* smem = smem_raw + ((1024u - (smem_addr(smem_raw) & 1023u)) & 1023u);
   float* sD = reinterpret_cast<float*>(smem + SMEM_EPI);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + SMEM_BAR);
   uint64_t* full = bars;                  // [NSTAGE] operands landed

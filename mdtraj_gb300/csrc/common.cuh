@@ -171,6 +171,21 @@ GB_DEV bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* err, uint32_t
   return false;
 }
 
+// try_wait with a suspend-time hint: the thread sleeps until the phase
+// completes or about hint_ns nanoseconds have passed, and issues nothing
+// meanwhile (a plain try_wait returns after a short hardware-defined time).
+GB_DEV bool mbar_try_wait_sleep(uint64_t* bar, uint32_t parity, uint32_t hint_ns) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity), "r"(hint_ns)
+      : "memory");
+  return ok != 0;
+}
+
 // Nanoseconds of the GPU's global timer.
 GB_DEV uint64_t global_ns() {
   uint64_t t;
@@ -190,6 +205,20 @@ GB_DEV bool mbar_wait_timed(uint64_t* bar, uint32_t parity, int* err, uint64_t l
 #pragma unroll 1
     for (int i = 0; i < 64; ++i)
       if (mbar_try_wait(bar, parity)) return true;
+    if (global_ns() - t0 > limit_ns) break;
+  }
+  if (err) atomicOr(err, DEV_ERR_TIMEOUT);
+  return false;
+}
+
+// The same bound with sleeping try_waits (1 ms hint each): for waits that
+// last a large part of a pipeline step, so that the waiting warps leave the
+// issue slots to the warps with work.  2^24 rounds stay as the backstop.
+GB_DEV bool mbar_wait_sleep(uint64_t* bar, uint32_t parity, int* err, uint64_t limit_ns) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = global_ns();
+  for (uint32_t round = 0; round < (1u << 24); ++round) {
+    if (mbar_try_wait_sleep(bar, parity, 1000000u)) return true;
     if (global_ns() - t0 > limit_ns) break;
   }
   if (err) atomicOr(err, DEV_ERR_TIMEOUT);
