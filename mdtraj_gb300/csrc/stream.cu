@@ -14,14 +14,16 @@
 //                      FP32 over one stage, then folds those into
 //                      error-free (TwoSum) float pairs.  A warp transpose
 //                      reduction turns the 13 sums into FP64 records.
-//   2. finish_kernel   one thread per frame: combines the split records in
+//   2. finish_refine_kernel
+//                      one thread per frame: combines the split records in
 //                      FP64 (exact re-centring), solves QCP in FP64 (Newton
 //                      on the quartic) and writes rmsd / centroid / trace.
 //                      Frames whose msd is below what the one-pass sums can
-//                      resolve (near-identical structures) are queued.
-//   3. refine_kernel   one warp per queued frame: msd = sum |R (a - mu) -
-//                      b|^2 / n with the QCP rotation, which has no
-//                      cancellation as rmsd -> 0.
+//                      resolve (near-identical structures) are then refined
+//                      by their warp: msd = sum |R (a - mu) - b|^2 / n with
+//                      the QCP rotation, which has no cancellation as
+//                      rmsd -> 0.  (The rotation call keeps the two-kernel
+//                      form, finish_kernel + refine_kernel over a queue.)
 //
 // Reference algorithm (CPU): mdtraj/rmsd/_rmsd.pyx:211-224 (centre, then
 // msd_atom_major per frame), src/center_generic.h:3-44 (centring),
@@ -31,6 +33,7 @@
 #include <math.h>
 #include <string.h>
 
+#include <algorithm>
 #include <atomic>
 
 #include "capi_internal.h"
@@ -389,68 +392,130 @@ struct RefineArgs {
   float* out_centroid;  // entries with seg = -1: centroid of a non-finite frame
 };
 
+// One queued frame, by the whole warp (every lane calls it with the same
+// entry): msd = sum |R (a - mu) - b|^2 / n with the entry's rotation and
+// split-float centroid, or (seg = -1) the centroid of a frame with
+// non-finite coordinates by plain FP64 sums.
+template <int LAYOUT>
+__device__ __forceinline__ void refine_one(const RefineArgs& r, const RefineEntry& en, int lane) {
+  constexpr int U = 4;  // quads in flight per lane (8 measured slower: more code to fetch cold)
+  const int32_t A = r.n_atoms, Ap = r.n_padded, Q = (A + 3) >> 2;
+  const float* fr = r.x + en.frame * r.frame_stride;
+  if (en.seg < 0) {
+    // centroid of a frame with non-finite coordinates as the reference
+    // computes it (src/center_generic.h: double sum, divide, round to
+    // float), which keeps +-inf where the shifted sums give NaN
+    double s[3] = {0.0, 0.0, 0.0};
+    for (int32_t q = lane; q < Q; q += 32) {
+      float ax[4], ay[4], az[4];
+      load_frame_quad<LAYOUT>(fr, Ap, q, ax, ay, az);
+      const int nv = A - 4 * q;
+#pragma unroll
+      for (int t = 0; t < 4; ++t)
+        if (t < nv) { s[0] += ax[t]; s[1] += ay[t]; s[2] += az[t]; }
+    }
+    for (int k = 0; k < 3; ++k) s[k] = warp_sum_d(s[k]);
+    if (lane == 0 && r.out_centroid)
+      for (int k = 0; k < 3; ++k) r.out_centroid[3 * en.frame + k] = (float)(s[k] / (double)A);
+    return;
+  }
+  CF acc = cf_zero();
+  int32_t q = lane;
+  for (; q + 32 * (U - 1) < Q; q += 32 * U) {
+    float ax[U][4], ay[U][4], az[U][4];
+#pragma unroll
+    for (int u = 0; u < U; ++u) load_frame_quad<LAYOUT>(fr, Ap, q + 32 * u, ax[u], ay[u], az[u]);
+    float part = 0.f;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      float bx[4], by[4], bz[4];
+      load_ref_quad<LAYOUT, false>(r.ref, Ap, q + 32 * u, bx, by, bz);
+      part += residual_quad(en, ax[u], ay[u], az[u], bx, by, bz, A - 4 * (q + 32 * u));
+    }
+    cf_add(acc, part);
+  }
+  for (; q < Q; q += 32) {
+    float ax[4], ay[4], az[4], bx[4], by[4], bz[4];
+    load_frame_quad<LAYOUT>(fr, Ap, q, ax, ay, az);
+    load_ref_quad<LAYOUT, false>(r.ref, Ap, q, bx, by, bz);
+    cf_add(acc, residual_quad(en, ax, ay, az, bx, by, bz, A - 4 * q));
+  }
+#pragma unroll
+  for (int m = 16; m >= 1; m >>= 1) {
+    CF o;
+    o.hi = __shfl_xor_sync(FULL_MASK, acc.hi, m);
+    o.lo = __shfl_xor_sync(FULL_MASK, acc.lo, m);
+    acc = cf_add2(acc, o);
+  }
+  if (lane == 0) {
+    // in FP32: the sum is exact to ~1e-12 and the output is a float (an FP64
+    // division and square root are long FP64 sequences on GB300)
+    float msd = __fadd_rn(acc.hi, acc.lo) * (1.0f / (float)A);
+    if (!(msd > 0.0f)) msd = 0.0f;
+    r.out_rmsd[en.frame] = sqrtf(msd);
+  }
+}
+
+// Refinement of a queue filled by finish_kernel: one warp per entry.
 template <int LAYOUT>
 __global__ void __launch_bounds__(256) refine_kernel(const RefineArgs r) {
-  constexpr int U = 4;  // quads in flight per lane
   const int lane = threadIdx.x & 31;
   const int64_t W = (int64_t)gridDim.x * (blockDim.x >> 5);
   const int64_t gw = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int n = *reinterpret_cast<const volatile int*>(r.count);
-  const int32_t A = r.n_atoms, Ap = r.n_padded, Q = (A + 3) >> 2;
-  for (int64_t e = gw; e < n; e += W) {
-    const RefineEntry en = r.list[e];
-    const float* fr = r.x + en.frame * r.frame_stride;
-    if (en.seg < 0) {
-      // centroid of a frame with non-finite coordinates as the reference
-      // computes it (src/center_generic.h: double sum, divide, round to
-      // float), which keeps +-inf where the shifted sums give NaN
-      double s[3] = {0.0, 0.0, 0.0};
-      for (int32_t q = lane; q < Q; q += 32) {
-        float ax[4], ay[4], az[4];
-        load_frame_quad<LAYOUT>(fr, Ap, q, ax, ay, az);
-        const int nv = A - 4 * q;
+  for (int64_t e = gw; e < n; e += W) refine_one<LAYOUT>(r, r.list[e], lane);
+}
+
+// Finish and refinement in one launch (the single-reference call): thread j
+// of block b finishes frame b * per_block + j; the frames of a warp that need
+// the refinement pass are then refined by that warp, one after the other
+// with all 32 lanes.  Blocks take equal shares of the frames, one block per
+// SM while there are at most 128 frames per SM: the FP64 QCP is the cost
+// here (GB300's FP64 pipe is narrow), so the SM with the most frames sets
+// the time, and a second launch for the refinement would cost as much again
+// as its (usually empty) work.
+template <int LAYOUT>
+__global__ void __launch_bounds__(128) finish_refine_kernel(const FinishArgs a, const RefineArgs r,
+                                                           int32_t per_block) {
+  const int j = threadIdx.x;
+  const int lane = j & 31;
+  const int64_t f = (int64_t)blockIdx.x * per_block + j;
+  RefineEntry held;
+  bool pending = false;
+  if (j < per_block && f < a.n_frames) {
+    FrameCtx c;
+    c.recs = a.sums + f * (int64_t)a.splits * SUMS_STRIDE;
+    c.S = a.splits;
+    c.A = a.n_atoms;
+    c.inv_a = a.inv_atoms;
+    c.mode = a.mode;
+    c.ref_info = a.ref_info;
+    c.ref_prefix = a.ref_prefix;
+    c.g_target = (a.mode == MODE_PRECENTERED) ? a.g_target[f] : 0.f;
+    c.g_ref = a.g_ref_override;
+    c.self = (f == a.self_index);
+    c.out_idx = f;
+    c.refine_frame = f;
+    c.refine_seg = 0;
+    c.out_rot = nullptr;
+    c.out_mu = nullptr;
+    finish_frame(c, a.out_rmsd, a.out_centroid, a.out_trace, nullptr, nullptr, a.err, &held, &pending);
+  }
+  unsigned todo = __ballot_sync(FULL_MASK, pending);
+  while (todo) {
+    const int src = __ffs(todo) - 1;
+    todo &= todo - 1;
+    RefineEntry en;
+    en.frame = __shfl_sync(FULL_MASK, held.frame, src);
 #pragma unroll
-        for (int t = 0; t < 4; ++t)
-          if (t < nv) { s[0] += ax[t]; s[1] += ay[t]; s[2] += az[t]; }
-      }
-      for (int k = 0; k < 3; ++k) s[k] = warp_sum_d(s[k]);
-      if (lane == 0 && r.out_centroid)
-        for (int k = 0; k < 3; ++k) r.out_centroid[3 * en.frame + k] = (float)(s[k] / (double)A);
-      continue;
-    }
-    CF acc = cf_zero();
-    int32_t q = lane;
-    for (; q + 32 * (U - 1) < Q; q += 32 * U) {
-      float ax[U][4], ay[U][4], az[U][4];
+    for (int i = 0; i < 9; ++i) en.rot[i] = __shfl_sync(FULL_MASK, held.rot[i], src);
 #pragma unroll
-      for (int u = 0; u < U; ++u) load_frame_quad<LAYOUT>(fr, Ap, q + 32 * u, ax[u], ay[u], az[u]);
-      float part = 0.f;
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        float bx[4], by[4], bz[4];
-        load_ref_quad<LAYOUT, false>(r.ref, Ap, q + 32 * u, bx, by, bz);
-        part += residual_quad(en, ax[u], ay[u], az[u], bx, by, bz, A - 4 * (q + 32 * u));
-      }
-      cf_add(acc, part);
+    for (int k = 0; k < 3; ++k) {
+      en.mu_hi[k] = __shfl_sync(FULL_MASK, held.mu_hi[k], src);
+      en.mu_lo[k] = __shfl_sync(FULL_MASK, held.mu_lo[k], src);
     }
-    for (; q < Q; q += 32) {
-      float ax[4], ay[4], az[4], bx[4], by[4], bz[4];
-      load_frame_quad<LAYOUT>(fr, Ap, q, ax, ay, az);
-      load_ref_quad<LAYOUT, false>(r.ref, Ap, q, bx, by, bz);
-      cf_add(acc, residual_quad(en, ax, ay, az, bx, by, bz, A - 4 * q));
-    }
-#pragma unroll
-    for (int m = 16; m >= 1; m >>= 1) {
-      CF o;
-      o.hi = __shfl_xor_sync(FULL_MASK, acc.hi, m);
-      o.lo = __shfl_xor_sync(FULL_MASK, acc.lo, m);
-      acc = cf_add2(acc, o);
-    }
-    if (lane == 0) {
-      double msd = cf_to_double(acc) / (double)A;
-      if (!(msd > 0.0)) msd = 0.0;
-      r.out_rmsd[en.frame] = (float)sqrt(msd);
-    }
+    en.seg = __shfl_sync(FULL_MASK, held.seg, src);
+    refine_one<LAYOUT>(r, en, lane);
   }
 }
 
@@ -945,28 +1010,28 @@ int gbrmsd_rmsd_to_reference(const float* x, int64_t n_frames, int32_t n_atoms, 
   fa.mode = mode;
   fa.out_rot = nullptr;
   fa.out_mu = nullptr;
-  launch_finish(fa, n_frames, st);
-  GB_CUDA_TRY(cudaGetLastError(), "launch finish_kernel");
 
-  if (mode != MODE_NOSUPERPOSE) {
-    RefineArgs ra;
-    ra.x = x;
-    ra.n_atoms = n_atoms;
-    ra.n_padded = n_padded;
-    ra.frame_stride = frame_stride;
-    ra.ref = sa.ref;
-    ra.list = fa.refine;
-    ra.count = fa.refine_count;
-    ra.out_rmsd = out_rmsd;
-    ra.out_centroid = out_centroid;
-    // one warp per queued frame; the queue is usually short or empty
-    const int rgrid = sm_count() * 2;
-    if (layout == ATOM_MAJOR)
-      refine_kernel<ATOM_MAJOR><<<rgrid, 256, 0, st>>>(ra);
-    else
-      refine_kernel<AXIS_MAJOR><<<rgrid, 256, 0, st>>>(ra);
-    GB_CUDA_TRY(cudaGetLastError(), "launch refine_kernel");
-  }
+  RefineArgs ra;
+  ra.x = x;
+  ra.n_atoms = n_atoms;
+  ra.n_padded = n_padded;
+  ra.frame_stride = frame_stride;
+  ra.ref = sa.ref;
+  ra.list = fa.refine;
+  ra.count = fa.refine_count;
+  ra.out_rmsd = out_rmsd;
+  ra.out_centroid = out_centroid;
+  // equal shares of at most 128 frames per block, one block per SM while
+  // they fit
+  const int64_t sms = sm_count();
+  const int32_t per_block = (int32_t)std::min<int64_t>(128, (n_frames + sms - 1) / sms);
+  const unsigned blocks = (unsigned)((n_frames + per_block - 1) / per_block);
+  const int threads = (per_block + 31) & ~31;
+  if (layout == ATOM_MAJOR)
+    finish_refine_kernel<ATOM_MAJOR><<<blocks, threads, 0, st>>>(fa, ra, per_block);
+  else
+    finish_refine_kernel<AXIS_MAJOR><<<blocks, threads, 0, st>>>(fa, ra, per_block);
+  GB_CUDA_TRY(cudaGetLastError(), "launch finish_refine_kernel");
   return GBRMSD_OK;
 }
 

@@ -227,7 +227,7 @@ __device__ __forceinline__ void accum_quad(float (&acc)[NV], const float (&ax)[4
 //   mu = sum_j (sd_j + n_j s_j) / A
 //   Ga = sum_j (g_j + 2 (s_j - mu) . sd_j + n_j |s_j - mu|^2)
 //   M  = sum_j (m_j + (s_j - mu) B_j^T),  B_j = sum of the reference over split j,
-// QCP (FP32 Newton + FP64 polish), outputs, and the refinement queue.
+// QCP (FP32 Newton + float-float polish), outputs, and the refinement queue.
 struct FrameCtx {
   const double* recs;      // S records of SUMS_STRIDE doubles
   int32_t S, A, mode;
@@ -244,8 +244,12 @@ struct FrameCtx {
   double* out_mu;          // optional with out_rot: FP64 centroid per frame, 3 doubles
 };
 
+// A frame that needs the refinement pass is queued in refine[] (refine_count
+// the queue's length), or, when `held` is given, handed back in *held with
+// *pending set, for the caller to refine at once.
 __device__ __forceinline__ void finish_frame(const FrameCtx& c, float* out_rmsd, float* out_centroid,
-                                             float* out_trace, RefineEntry* refine, int* refine_count, int* err) {
+                                             float* out_trace, RefineEntry* refine, int* refine_count, int* err,
+                                             RefineEntry* held = nullptr, bool* pending = nullptr) {
   const int32_t A = c.A, S = c.S;
   const int32_t Q = (A + 3) >> 2;
   const double* base = c.recs;
@@ -324,7 +328,7 @@ __device__ __forceinline__ void finish_frame(const FrameCtx& c, float* out_rmsd,
     out_rmsd[f] = 0.f;
     if (c.out_rot)
       for (int i = 0; i < 9; ++i) c.out_rot[9 * f + i] = nanf("");
-    if (out_centroid && refine && c.mode == MODE_CENTER) {
+    if (out_centroid && (refine || held) && c.mode == MODE_CENTER) {
       // The shifted one-pass sums turn an infinite coordinate into NaN, where
       // the reference's double sum gives +-inf: the refinement pass recomputes
       // this frame's centroid by plain FP64 sums (marked by seg = -1).
@@ -333,12 +337,19 @@ __device__ __forceinline__ void finish_frame(const FrameCtx& c, float* out_rmsd,
       for (int i = 0; i < 9; ++i) e.rot[i] = 0.f;
       for (int k = 0; k < 3; ++k) { e.mu_hi[k] = 0.f; e.mu_lo[k] = 0.f; }
       e.seg = -1;
-      refine[atomicAdd(refine_count, 1)] = e;
+      if (held) {
+        *held = e;
+        *pending = true;
+      } else {
+        refine[atomicAdd(refine_count, 1)] = e;
+      }
     }
     return;
   }
   int iters = 0;
-  const double lam = qcp_lambda_max_mixed(m, ga, gb, &iters);
+  bool short_ = false;
+  double lam = qcp_lambda_max_df(m, ga, gb, &iters, &short_);
+  if (short_) lam = qcp_newton_fp64(m, lam);  // (near) double root: rare, FP64
   double msd = (ga + gb - 2.0 * lam) * invA;
   if (!(msd > 0.0) || self) msd = 0.0;
   out_rmsd[f] = sqrtf((float)msd);
@@ -356,18 +367,20 @@ __device__ __forceinline__ void finish_frame(const FrameCtx& c, float* out_rmsd,
   // refinement kernel.  scale = (G_a + G_b) / (2 A).
   const double scale = (ga + gb) * (0.5 * invA);
   if (msd * dA < 0.01 * scale * scale && A > 0) {
-    double rot[9];
-    qcp_rotation(m, lam, rot);
-    const int slot = atomicAdd(refine_count, 1);
     RefineEntry e;
+    qcp_rotation_refine(m, lam, e.rot);
     e.frame = c.refine_frame;
-    for (int i = 0; i < 9; ++i) e.rot[i] = (float)rot[i];
     for (int k = 0; k < 3; ++k) {
       e.mu_hi[k] = (float)mu[k];
       e.mu_lo[k] = (float)(mu[k] - (double)e.mu_hi[k]);
     }
     e.seg = c.refine_seg;
-    refine[slot] = e;
+    if (held) {
+      *held = e;
+      *pending = true;
+    } else {
+      refine[atomicAdd(refine_count, 1)] = e;
+    }
   }
 }
 

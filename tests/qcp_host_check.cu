@@ -5,7 +5,9 @@
 // coordinates of the moving frame a and the reference frame b).  For each
 // case prints: lambda (mixed FP32/FP64 solve), lambda (FP64 solve), the
 // upper bound (Ga + Gb) / 2, the QCP msd, whether the finish would refine
-// the frame, and the direct residual rmsd with the QCP rotation.
+// the frame, the direct residual rmsd with the QCP rotation, lambda from
+// the float-float solve (the one the finish kernels use), and the direct
+// residual rmsd with the refinement pass's FP32 rotation.
 #include <cmath>
 #include <cstdio>
 
@@ -45,12 +47,16 @@ int main() {
     int it1 = 0, it2 = 0;
     const double lam = qcp_lambda_max_mixed(m, ga, gb, &it1);
     const double lam64 = qcp_lambda_max(m, ga, gb, &it2);
-    double msd = (ga + gb - 2.0 * lam) / A;
+    int it3 = 0;
+    bool short_ = false;
+    double lamdf = qcp_lambda_max_df(m, ga, gb, &it3, &short_);
+    if (short_) lamdf = qcp_newton_fp64(m, lamdf);
+    double msd = (ga + gb - 2.0 * lamdf) / A;
     if (!(msd > 0.0)) msd = 0.0;
     const double scale = (ga + gb) * 0.5 / A;
     const int refine = msd * A < 0.01 * scale * scale;
     double rot[9];
-    qcp_rotation(m, lam, rot);
+    qcp_rotation(m, lamdf, rot);
     double s = 0.0;
     for (int k = 0; k < A; ++k) {
       double x[3], y[3];
@@ -63,7 +69,22 @@ int main() {
         s += r * r;
       }
     }
-    std::printf("%.17g %.17g %.17g %.17g %d %.17g\n", lam, lam64, 0.5 * (ga + gb), msd, refine, std::sqrt(s / A));
+    float rf[9];
+    qcp_rotation_refine(m, lamdf, rf);
+    double s2 = 0.0;
+    for (int k = 0; k < A; ++k) {
+      double x[3], y[3];
+      for (int c = 0; c < 3; ++c) {
+        x[c] = a[k][c] - ma[c];
+        y[c] = b[k][c] - mb[c];
+      }
+      for (int i = 0; i < 3; ++i) {
+        const double r = rf[3 * i] * x[0] + rf[3 * i + 1] * x[1] + rf[3 * i + 2] * x[2] - y[i];
+        s2 += r * r;
+      }
+    }
+    std::printf("%.17g %.17g %.17g %.17g %d %.17g %.17g %.17g\n", lam, lam64, 0.5 * (ga + gb), msd, refine,
+                std::sqrt(s / A), lamdf, std::sqrt(s2 / A));
   }
   return 0;
 }
