@@ -305,6 +305,18 @@ int gbrmsd_center_inplace(float* x, int64_t n_frames, int32_t n_atoms, int32_t n
                           int64_t frame_stride, int32_t layout, float* out_traces,
                           float* out_centroids, void* ws, size_t ws_bytes, void* stream);
 
+/* Mass-weighted centring: replaces the mass_weighted=True branch of
+ * Trajectory.center_coordinates (mdtraj/core/trajectory.py:2133-2134, with
+ * compute_center_of_mass, mdtraj/geometry/distance.py:366-384).  x is
+ * atom-major (frame_stride floats apart, no padding needed); weights are the
+ * n_atoms normalised masses (doubles, device, summing to 1 as the reference
+ * normalises them).  Per frame com = sum_k w_k x_k (to ~2^-48 relative) and
+ * x <- float(x - com) in place; out_com (n_frames x 3 doubles, device) may be
+ * null.  No workspace; traces are not computed (the reference's assignment
+ * to xyz drops them). */
+int gbrmsd_center_weighted_inplace(float* x, int64_t n_frames, int32_t n_atoms, int64_t frame_stride,
+                                   const double* weights, double* out_com, void* stream);
+
 /* Synchronises `stream` and returns GBRMSD_E_DEVICE if a kernel that used
  * this workspace recorded a device-side error (e.g. a bounded wait expired),
  * GBRMSD_OK otherwise.  The error word is cleared by the next call.

@@ -89,11 +89,11 @@ def frames_to_device(x: np.ndarray, layout: int, device, stream: int) -> tuple[t
         rows, hrow, drow = _rows(layout, F, A)
         if pageable_access():
             check(lib.gbrmsd_copy_rows_kernel(buf.data_ptr(), drow, x.ctypes.data, hrow, hrow, drow, rows, stream))
-            if x is not src:
-                # the kernel reads the host array asynchronously: a converted
-                # copy made here must outlive it (the caller's own array is
-                # the caller's to keep alive until it synchronises)
-                torch.cuda.synchronize(device)
+            # the kernel reads the host pages asynchronously: wait for it, so
+            # that the array (the caller's, or a converted copy made here) may
+            # be dropped as soon as this returns -- a kernel reading pages
+            # that were unmapped in the meantime faults the GPU
+            torch.cuda.ExternalStream(stream, device=device).synchronize()
         else:
             copy_rows(buf.data_ptr(), drow * 4, x.ctypes.data, hrow * 4, hrow * 4, rows, 1, stream)
     return buf, Ap

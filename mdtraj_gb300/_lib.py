@@ -74,6 +74,7 @@ SIGNATURES: dict[str, tuple] = {
     "gbrmsd_ragged_setup": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     "gbrmsd_ragged_rmsd": (C.c_int, [_vp, _vp, _vp, _vp, _sz, _vp]),
     "gbrmsd_center_inplace": (C.c_int, [_vp, _i64, _i32, _i32, _i64, _i32, _vp, _vp, _vp, _sz, _vp]),
+    "gbrmsd_center_weighted_inplace": (C.c_int, [_vp, _i64, _i32, _i64, _vp, _vp, _vp]),
     "gbrmsd_workspace_status": (C.c_int, [_vp, _vp]),
     "gbrmsd_workspace_error_word": (C.c_int, [_vp, _vp, _vp]),
     "gbrmsd_noalloc_status": (C.c_int, [_vp, _vp]),

@@ -263,6 +263,31 @@ def _center_inplace_atom_major(xyz):
     return D.to_host(traces, stream)
 
 
+def _center_weighted_inplace_atom_major(xyz, weights) -> None:
+    """Subtracts each frame's weighted centre sum_k w_k x_k from a float32
+    C-contiguous (n_frames, n_atoms, 3) array in place: the work of
+    ``xyz -= compute_center_of_mass(traj)[:, None, :]`` in
+    Trajectory.center_coordinates(mass_weighted=True)
+    (mdtraj/core/trajectory.py:2133-2134; mdtraj/geometry/distance.py:366-384),
+    with ``weights`` the masses already normalised to sum 1."""
+    xyz = _memview3(xyz, "xyz")
+    assert xyz.shape[2] == 3
+    n_frames, n_atoms = xyz.shape[0], xyz.shape[1]
+    w = np.ascontiguousarray(weights, dtype=np.float64)
+    if w.shape != (n_atoms,):
+        raise ValueError(f"weights must have shape ({n_atoms},), got {w.shape}")
+    if n_frames == 0 or n_atoms == 0:
+        return
+    device = D.require_device()
+    stream = D.stream_handle()
+    x_dev, n_padded = D.frames_to_device(xyz, _lib.ATOM_MAJOR, device, stream)
+    w_dev = torch.from_numpy(w).to(device)
+    check(lib.gbrmsd_center_weighted_inplace(x_dev.data_ptr(), n_frames, n_atoms, 3 * n_padded, w_dev.data_ptr(),
+                                             None, stream))
+    D.frames_to_host(x_dev, xyz, _lib.ATOM_MAJOR, n_atoms, n_padded, stream)
+    torch.cuda.current_stream().synchronize()
+
+
 # superposition entry points of the same module (_rmsd.pyx:246-759); imported
 # last because they use the argument coercions above
 from .superpose import getMultipleAlignDisplaceRMSDs_atom_major, rmsf, superpose_atom_major  # noqa: E402,F401

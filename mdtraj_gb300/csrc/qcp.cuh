@@ -282,22 +282,19 @@ __host__ __device__ __forceinline__ double qcp_newton_fp64(const double* m, doub
 // lambda_max as qcp_lambda_max_mixed, on float-float coefficients: FP32
 // Newton on the normalised quartic, then float-float Newton steps on P
 // (float-float P, float P') until P reaches its rounding floor or the step
-// is below 2^-44 lambda.  Inputs are converted once (33 FP64 operations).
+// is below 2^-44 lambda.  M and lam0 = (G_a + G_b) / 2 come as float pairs
+// and lambda is returned as one: no FP64 instruction at all.
 // At a (near) double largest root, as for (nearly) collinear structures,
 // Newton converges only linearly and P's floor stops it ~sqrt(2^-44) ~ 1e-6
 // (relative) short of the root, 8x further than FP64's floor does; *short_
 // is then set (the last step was still above 1e-9 lambda, or the steps ran
 // out) and the caller polishes with qcp_newton_fp64.
-__host__ __device__ __forceinline__ double qcp_lambda_max_df(const double* md, double gad, double gbd, int* iters,
-                                                             bool* short_, int max_iter = 24) {
+__host__ __device__ __forceinline__ DF qcp_lambda_max_dfm(const DF (&m)[9], DF lam0, int* iters, bool* short_,
+                                                         int max_iter = 24) {
   *short_ = false;
-  DF m[9];
-#pragma unroll
-  for (int i = 0; i < 9; ++i) m[i] = df_from_double(md[i]);
-  const DF lam0 = df_mul_f(df_add(df_from_double(gad), df_from_double(gbd)), 0.5f);
   if (!(lam0.hi > 0.0f)) {
     if (iters) *iters = 0;
-    return 0.0;
+    return DF{0.0f, 0.0f};
   }
   // K (theobald_rmsd.cpp:227-236 entry layout)
   const DF k00 = df_add(df_add(m[0], m[4]), m[8]), k01 = df_sub(m[5], m[7]), k02 = df_sub(m[6], m[2]);
@@ -354,9 +351,12 @@ __host__ __device__ __forceinline__ double qcp_lambda_max_df(const double* md, d
     if (!(dp != 0.0f)) break;
     // P at its rounding floor (~2^-44 of its terms): lam is a root to
     // working precision; at a double root P' is noise too and a step would
-    // be noise over noise
+    // be noise over noise.  Converged when the last step was already tiny
+    // or the Newton correction P / P' is (a simple root reached in one
+    // step, as from FP32 Newton's 1e-7 start); at a (near) double root P'
+    // is as small as P's noise allows and the correction stays large.
     if (fabsf(pv.hi) <= 4.5e-13f * (l2f * l2f + fabsf(c2.hi) * l2f + fabsf(c1.hi * lf) + fabsf(c0.hi))) {
-      done = !(fabsf(last) > 1e-9f * fabsf(lf));
+      done = !(fabsf(last) > 1e-9f * fabsf(lf)) || fabsf(pv.hi + pv.lo) <= 1e-9f * fabsf(lf * dp);
       break;
     }
     const float step = (pv.hi + pv.lo) / dp;
@@ -370,7 +370,17 @@ __host__ __device__ __forceinline__ double qcp_lambda_max_df(const double* md, d
   }
   *short_ = !done;
   if (iters) *iters = it + jt;
-  return df_to_double(lam);
+  return lam;
+}
+
+// The same from FP64 inputs, converted once (33 FP64 operations).
+__host__ __device__ __forceinline__ double qcp_lambda_max_df(const double* md, double gad, double gbd, int* iters,
+                                                             bool* short_, int max_iter = 24) {
+  DF m[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) m[i] = df_from_double(md[i]);
+  const DF lam0 = df_mul_f(df_add(df_from_double(gad), df_from_double(gbd)), 0.5f);
+  return df_to_double(qcp_lambda_max_dfm(m, lam0, iters, short_, max_iter));
 }
 
 // Rotation R (row-major) minimising sum_k |R a_k - b_k|^2 for the given

@@ -13,17 +13,20 @@
 //                      inner product, the coordinate sum and the trace in
 //                      FP32 over one stage, then folds those into
 //                      error-free (TwoSum) float pairs.  A warp transpose
-//                      reduction turns the 13 sums into FP64 records.
-//   2. finish_refine_kernel
-//                      one thread per frame: combines the split records in
-//                      FP64 (exact re-centring), solves QCP in FP64 (Newton
-//                      on the quartic) and writes rmsd / centroid / trace.
-//                      Frames whose msd is below what the one-pass sums can
-//                      resolve (near-identical structures) are then refined
-//                      by their warp: msd = sum |R (a - mu) - b|^2 / n with
-//                      the QCP rotation, which has no cancellation as
-//                      rmsd -> 0.  (The rotation call keeps the two-kernel
-//                      form, finish_kernel + refine_kernel over a queue.)
+//                      reduction turns the 13 sums into one record per unit.
+//   2. the finish      one thread per frame: combines the split records
+//                      (exact re-centring), solves QCP (Newton on the
+//                      quartic) and writes rmsd / centroid / trace.  Frames
+//                      whose msd is below what the one-pass sums can resolve
+//                      (near-identical structures) are then refined by a
+//                      whole warp: msd = sum |R (a - mu) - b|^2 / n with the
+//                      QCP rotation, which has no cancellation as rmsd -> 0.
+//                      With one unit per frame (the usual case) the finish
+//                      runs at the end of stream_kernel itself, in float-pair
+//                      arithmetic, 32 frames per warp (stream_fin_tail);
+//                      otherwise finish_refine_kernel runs it on FP64
+//                      records.  (The rotation call keeps the two-kernel form,
+//                      finish_kernel + refine_kernel over a queue.)
 //
 // Reference algorithm (CPU): mdtraj/rmsd/_rmsd.pyx:211-224 (centre, then
 // msd_atom_major per frame), src/center_generic.h:3-44 (centring),
@@ -56,6 +59,86 @@ __global__ void __launch_bounds__(PREP_THREADS) ref_prepare_kernel(
   __shared__ double red[32];
   __shared__ double part[PREP_THREADS * 3];
   prepare_reference_block(raw, A, Ap, layout, centre, out, info, prefix, red, part);
+}
+
+// ---------------------------------------------------------------------------
+// Refinement: direct residual for near-identical frames (warp per frame)
+// ---------------------------------------------------------------------------
+
+struct RefineArgs {
+  const float* x;
+  int32_t n_atoms;
+  int32_t n_padded;
+  int64_t frame_stride;
+  const float* ref;
+  const RefineEntry* list;
+  const int* count;
+  float* out_rmsd;
+  float* out_centroid;  // entries with seg = -1: centroid of a non-finite frame
+};
+
+// One queued frame, by the whole warp (every lane calls it with the same
+// entry): msd = sum |R (a - mu) - b|^2 / n with the entry's rotation and
+// split-float centroid, or (seg = -1) the centroid of a frame with
+// non-finite coordinates by plain FP64 sums.
+template <int LAYOUT>
+__device__ __forceinline__ void refine_one(const RefineArgs& r, const RefineEntry& en, int lane) {
+  constexpr int U = 4;  // quads in flight per lane (8 measured slower: more code to fetch cold)
+  const int32_t A = r.n_atoms, Ap = r.n_padded, Q = (A + 3) >> 2;
+  const float* fr = r.x + en.frame * r.frame_stride;
+  if (en.seg < 0) {
+    // centroid of a frame with non-finite coordinates as the reference
+    // computes it (src/center_generic.h: double sum, divide, round to
+    // float), which keeps +-inf where the shifted sums give NaN
+    double s[3] = {0.0, 0.0, 0.0};
+    for (int32_t q = lane; q < Q; q += 32) {
+      float ax[4], ay[4], az[4];
+      load_frame_quad<LAYOUT>(fr, Ap, q, ax, ay, az);
+      const int nv = A - 4 * q;
+#pragma unroll
+      for (int t = 0; t < 4; ++t)
+        if (t < nv) { s[0] += ax[t]; s[1] += ay[t]; s[2] += az[t]; }
+    }
+    for (int k = 0; k < 3; ++k) s[k] = warp_sum_d(s[k]);
+    if (lane == 0 && r.out_centroid)
+      for (int k = 0; k < 3; ++k) r.out_centroid[3 * en.frame + k] = (float)(s[k] / (double)A);
+    return;
+  }
+  CF acc = cf_zero();
+  int32_t q = lane;
+  for (; q + 32 * (U - 1) < Q; q += 32 * U) {
+    float ax[U][4], ay[U][4], az[U][4];
+#pragma unroll
+    for (int u = 0; u < U; ++u) load_frame_quad<LAYOUT>(fr, Ap, q + 32 * u, ax[u], ay[u], az[u]);
+    float part = 0.f;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      float bx[4], by[4], bz[4];
+      load_ref_quad<LAYOUT, false>(r.ref, Ap, q + 32 * u, bx, by, bz);
+      part += residual_quad(en, ax[u], ay[u], az[u], bx, by, bz, A - 4 * (q + 32 * u));
+    }
+    cf_add(acc, part);
+  }
+  for (; q < Q; q += 32) {
+    float ax[4], ay[4], az[4], bx[4], by[4], bz[4];
+    load_frame_quad<LAYOUT>(fr, Ap, q, ax, ay, az);
+    load_ref_quad<LAYOUT, false>(r.ref, Ap, q, bx, by, bz);
+    cf_add(acc, residual_quad(en, ax, ay, az, bx, by, bz, A - 4 * q));
+  }
+#pragma unroll
+  for (int m = 16; m >= 1; m >>= 1) {
+    CF o;
+    o.hi = __shfl_xor_sync(FULL_MASK, acc.hi, m);
+    o.lo = __shfl_xor_sync(FULL_MASK, acc.lo, m);
+    acc = cf_add2(acc, o);
+  }
+  if (lane == 0) {
+    // in FP32: the sum is exact to ~1e-12 and the output is a float (an FP64
+    // division and square root are long FP64 sequences on GB300)
+    float msd = __fadd_rn(acc.hi, acc.lo) * (1.0f / (float)A);
+    if (!(msd > 0.0f)) msd = 0.0f;
+    r.out_rmsd[en.frame] = sqrtf(msd);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -116,14 +199,126 @@ __device__ __forceinline__ void issue_chunk(const StreamArgs& p, const void* tma
   }
 }
 
+// In-kernel finish (FIN), used when every frame is one unit (S = 1): after
+// its last frame each warp meets the rest of its CTA at a barrier, and the
+// CTA solves QCP for all of its frames, 32 at a time (one frame per lane,
+// finish_frame_df: no FP64 on the common path), spread over its warps, so
+// that a 10,000-frame call ends one QCP latency (~2-3 us) after its last
+// byte is read instead of a second launch later.  Frames that need the direct
+// residual are queued in the CTA's slice of the refinement list and refined
+// after a second barrier, one after another, each by the whole CTA.
+//
+// CTA-local frame i of CTA b belongs to warp w = i % WARPS, round
+// r = i / WARPS: unit b * WARPS + w + r * W (W warps in the grid).
+struct FinSlice {
+  int64_t n;     // frames of this CTA
+  int64_t base;  // first refinement-list entry of this CTA (frames of lower CTAs)
+};
+
+__device__ __forceinline__ FinSlice fin_slice(int64_t F, int warps) {
+  const int64_t W = (int64_t)gridDim.x * warps;
+  const int64_t b0 = (int64_t)blockIdx.x * warps;
+  const int64_t full = F / W, rem = F - full * W;
+  FinSlice s;
+  s.n = full * warps + min((int64_t)warps, max((int64_t)0, rem - b0));
+  s.base = full * warps * (int64_t)blockIdx.x + min(rem, b0);
+  return s;
+}
+
+// Direct residual of one queued frame by the whole CTA (WARPS warps): every
+// thread takes quads t, t + T, ... (T = WARPS * 32, up to 4 in flight), each
+// warp reduces its compensated partial, and thread 0 sums the WARPS partials
+// in warp order (deterministic).  One CTA-wide pass of a 1,000-atom frame is
+// a single round trip to memory; a warp alone needs several.
+template <int LAYOUT, int WARPS>
+__device__ __forceinline__ void refine_one_cta(const RefineArgs& r, const RefineEntry& en, CF* part, int warp,
+                                               int lane) {
+  constexpr int U = 4;
+  constexpr int T = WARPS * 32;
+  const int32_t A = r.n_atoms, Ap = r.n_padded, Q = (A + 3) >> 2;
+  const float* fr = r.x + en.frame * r.frame_stride;
+  CF acc = cf_zero();
+  int32_t q = threadIdx.x;
+  for (; q + T * (U - 1) < Q; q += T * U) {
+    float ax[U][4], ay[U][4], az[U][4];
+#pragma unroll
+    for (int u = 0; u < U; ++u) load_frame_quad<LAYOUT>(fr, Ap, q + T * u, ax[u], ay[u], az[u]);
+    float pp = 0.f;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      float bx[4], by[4], bz[4];
+      load_ref_quad<LAYOUT, false>(r.ref, Ap, q + T * u, bx, by, bz);
+      pp += residual_quad(en, ax[u], ay[u], az[u], bx, by, bz, A - 4 * (q + T * u));
+    }
+    cf_add(acc, pp);
+  }
+  for (; q < Q; q += T) {
+    float ax[4], ay[4], az[4], bx[4], by[4], bz[4];
+    load_frame_quad<LAYOUT>(fr, Ap, q, ax, ay, az);
+    load_ref_quad<LAYOUT, false>(r.ref, Ap, q, bx, by, bz);
+    cf_add(acc, residual_quad(en, ax, ay, az, bx, by, bz, A - 4 * q));
+  }
+#pragma unroll
+  for (int m = 16; m >= 1; m >>= 1) {
+    CF o;
+    o.hi = __shfl_xor_sync(FULL_MASK, acc.hi, m);
+    o.lo = __shfl_xor_sync(FULL_MASK, acc.lo, m);
+    acc = cf_add2(acc, o);
+  }
+  if (lane == 0) part[warp] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    CF sum = part[0];
+    for (int w = 1; w < WARPS; ++w) sum = cf_add2(sum, part[w]);
+    // in FP32, as refine_one
+    float msd = __fadd_rn(sum.hi, sum.lo) * (1.0f / (float)A);
+    if (!(msd > 0.0f)) msd = 0.0f;
+    r.out_rmsd[en.frame] = sqrtf(msd);
+  }
+  __syncthreads();  // part[] is reused by the next entry
+}
+
+// Called by every thread of the CTA once its records are written and
+// visible (after a __syncthreads).
+template <int LAYOUT, int WARPS>
+__device__ __noinline__ void stream_fin_tail(const FinishArgs& a, const RefineArgs& r, int* nref, int warp,
+                                             int lane) {
+  const FinSlice sl = fin_slice(a.n_frames, WARPS);
+  const int64_t W = (int64_t)gridDim.x * WARPS;
+  const int64_t b0 = (int64_t)blockIdx.x * WARPS;
+  const DF inv = DF{a.inv_hi, a.inv_lo};
+  for (int64_t k = warp; k * 32 < sl.n; k += WARPS) {
+    const int64_t i = k * 32 + lane;
+    RefineEntry held;
+    bool pending = false;
+    if (i < sl.n) {
+      const int64_t f = b0 + (i % WARPS) + (i / WARPS) * W;
+      finish_frame_df(reinterpret_cast<const float*>(a.sums + f * SUMS_STRIDE), f, a, inv, &held, &pending);
+    }
+    if (pending) a.refine[sl.base + atomicAdd_block(nref, 1)] = held;
+  }
+  __syncthreads();
+  const int n = *reinterpret_cast<volatile int*>(nref);
+  __shared__ CF part[WARPS];
+  for (int e = 0; e < n; ++e) {
+    const RefineEntry en = a.refine[sl.base + e];
+    if (en.seg >= 0) refine_one_cta<LAYOUT, WARPS>(r, en, part, warp, lane);  // same entry CTA-wide: uniform
+  }
+  // non-finite frames' centroids (plain FP64 sums), a warp each
+  for (int e = warp; e < n; e += WARPS)
+    if (a.refine[sl.base + e].seg < 0) refine_one<LAYOUT>(r, a.refine[sl.base + e], lane);
+}
+
 // Streaming pass.  WARPS warps per CTA, each with a private ring of NSTAGE
 // shared-memory stages of CQ quads, fed by bulk async copies that lane 0
 // issues NSTAGE chunks ahead.  FP32 level-1 sums cover at most 4 quads per
 // lane (16 atoms) before they are folded into TwoSum pairs, which bounds the
 // rounding error of the one-pass sums independently of the atom count.
-template <int LAYOUT, int MODE, int CQ, int NSTAGE, bool REF_SMEM, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32, 1) stream_kernel(const StreamArgs p,
-                                                               const __grid_constant__ CUtensorMap tmap) {
+// With FIN the call's finish runs at the end of the kernel (stream_fin_tail).
+template <int LAYOUT, int MODE, int CQ, int NSTAGE, bool REF_SMEM, int WARPS, bool FIN>
+__global__ void __launch_bounds__(WARPS * 32, 1)
+    stream_kernel(const StreamArgs p, const __grid_constant__ CUtensorMap tmap, const FinishArgs fa,
+                  const RefineArgs ra) {
   extern __shared__ __align__(128) unsigned char smem[];
   constexpr int STAGE_BYTES = CQ * 48;
   constexpr int NV = NSums<MODE>::value;
@@ -141,6 +336,8 @@ __global__ void __launch_bounds__(WARPS * 32, 1) stream_kernel(const StreamArgs 
   unsigned char* stages = smem + ref_al + (size_t)warp * NSTAGE * STAGE_BYTES;
   uint64_t* bars =
       reinterpret_cast<uint64_t*>(smem + ref_al + (size_t)WARPS * NSTAGE * STAGE_BYTES) + warp * NSTAGE;
+  // FIN: refinement entries the CTA's finish queued
+  int* fin_nref = reinterpret_cast<int*>(smem + ref_al + (size_t)WARPS * NSTAGE * (STAGE_BYTES + 8));
 
   if constexpr (REF_SMEM && USE_REF) {
     const float4* src = reinterpret_cast<const float4*>(p.ref);
@@ -152,6 +349,8 @@ __global__ void __launch_bounds__(WARPS * 32, 1) stream_kernel(const StreamArgs 
     for (int s = 0; s < NSTAGE; ++s) mbar_init(&bars[s], 1);
     fence_mbar_init();
   }
+  if constexpr (FIN)
+    if (threadIdx.x == 0) *fin_nref = 0;
   __syncthreads();
   const float* rbase = REF_SMEM ? sref : p.ref;
 
@@ -313,12 +512,29 @@ __global__ void __launch_bounds__(WARPS * 32, 1) stream_kernel(const StreamArgs 
         for (int j = 0; j < 16; ++j) v[j] = (j < NV) ? acc2[j < NV ? j : 0] : cf_zero();
         warp_xpose_reduce16(v, lane);
         const int idx = lane >> 1;
-        if ((lane & 1) == 0 && idx < NV) rec[idx] = cf_to_double(v[0]);
+        if ((lane & 1) == 0 && idx < NV) {
+          if constexpr (FIN) {
+            // float pair (finish_frame_df's record), normalised
+            const DF d = df_two_sum(v[0].hi, v[0].lo);
+            float* recf = reinterpret_cast<float*>(rec);
+            recf[2 * idx] = d.hi;
+            recf[2 * idx + 1] = d.lo;
+          } else {
+            rec[idx] = cf_to_double(v[0]);
+          }
+        }
       }
       if (lane == 0 && MODE == MODE_CENTER) {
-        rec[16] = shift[0];
-        rec[17] = shift[1];
-        rec[18] = shift[2];
+        if constexpr (FIN) {
+          float* recf = reinterpret_cast<float*>(rec);
+          recf[DFREC_SHIFT] = shift[0];
+          recf[DFREC_SHIFT + 1] = shift[1];
+          recf[DFREC_SHIFT + 2] = shift[2];
+        } else {
+          rec[16] = shift[0];
+          rec[17] = shift[1];
+          rec[18] = shift[2];
+        }
       }
     }
   }
@@ -334,6 +550,12 @@ __global__ void __launch_bounds__(WARPS * 32, 1) stream_kernel(const StreamArgs 
       phases ^= 1u << slot;
       slot = (slot + 1 == NSTAGE) ? 0 : slot + 1;
     }
+  }
+  if constexpr (FIN) {
+    // every record of the CTA is written (a warp whose wait ran out leaves
+    // some unwritten: the error word already marks the call's results)
+    __syncthreads();
+    stream_fin_tail<LAYOUT, WARPS>(fa, ra, fin_nref, warp, lane);
   }
 }
 
@@ -374,86 +596,6 @@ __global__ void __launch_bounds__(256) finish_kernel(const FinishArgs a) {
 void launch_finish(const FinishArgs& fa, int64_t n_frames, cudaStream_t st) {
   const int t = finish_threads(n_frames);
   finish_kernel<<<(unsigned)((n_frames + t - 1) / t), t, 0, st>>>(fa);
-}
-
-// ---------------------------------------------------------------------------
-// Refinement: direct residual for near-identical frames (warp per frame)
-// ---------------------------------------------------------------------------
-
-struct RefineArgs {
-  const float* x;
-  int32_t n_atoms;
-  int32_t n_padded;
-  int64_t frame_stride;
-  const float* ref;
-  const RefineEntry* list;
-  const int* count;
-  float* out_rmsd;
-  float* out_centroid;  // entries with seg = -1: centroid of a non-finite frame
-};
-
-// One queued frame, by the whole warp (every lane calls it with the same
-// entry): msd = sum |R (a - mu) - b|^2 / n with the entry's rotation and
-// split-float centroid, or (seg = -1) the centroid of a frame with
-// non-finite coordinates by plain FP64 sums.
-template <int LAYOUT>
-__device__ __forceinline__ void refine_one(const RefineArgs& r, const RefineEntry& en, int lane) {
-  constexpr int U = 4;  // quads in flight per lane (8 measured slower: more code to fetch cold)
-  const int32_t A = r.n_atoms, Ap = r.n_padded, Q = (A + 3) >> 2;
-  const float* fr = r.x + en.frame * r.frame_stride;
-  if (en.seg < 0) {
-    // centroid of a frame with non-finite coordinates as the reference
-    // computes it (src/center_generic.h: double sum, divide, round to
-    // float), which keeps +-inf where the shifted sums give NaN
-    double s[3] = {0.0, 0.0, 0.0};
-    for (int32_t q = lane; q < Q; q += 32) {
-      float ax[4], ay[4], az[4];
-      load_frame_quad<LAYOUT>(fr, Ap, q, ax, ay, az);
-      const int nv = A - 4 * q;
-#pragma unroll
-      for (int t = 0; t < 4; ++t)
-        if (t < nv) { s[0] += ax[t]; s[1] += ay[t]; s[2] += az[t]; }
-    }
-    for (int k = 0; k < 3; ++k) s[k] = warp_sum_d(s[k]);
-    if (lane == 0 && r.out_centroid)
-      for (int k = 0; k < 3; ++k) r.out_centroid[3 * en.frame + k] = (float)(s[k] / (double)A);
-    return;
-  }
-  CF acc = cf_zero();
-  int32_t q = lane;
-  for (; q + 32 * (U - 1) < Q; q += 32 * U) {
-    float ax[U][4], ay[U][4], az[U][4];
-#pragma unroll
-    for (int u = 0; u < U; ++u) load_frame_quad<LAYOUT>(fr, Ap, q + 32 * u, ax[u], ay[u], az[u]);
-    float part = 0.f;
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      float bx[4], by[4], bz[4];
-      load_ref_quad<LAYOUT, false>(r.ref, Ap, q + 32 * u, bx, by, bz);
-      part += residual_quad(en, ax[u], ay[u], az[u], bx, by, bz, A - 4 * (q + 32 * u));
-    }
-    cf_add(acc, part);
-  }
-  for (; q < Q; q += 32) {
-    float ax[4], ay[4], az[4], bx[4], by[4], bz[4];
-    load_frame_quad<LAYOUT>(fr, Ap, q, ax, ay, az);
-    load_ref_quad<LAYOUT, false>(r.ref, Ap, q, bx, by, bz);
-    cf_add(acc, residual_quad(en, ax, ay, az, bx, by, bz, A - 4 * q));
-  }
-#pragma unroll
-  for (int m = 16; m >= 1; m >>= 1) {
-    CF o;
-    o.hi = __shfl_xor_sync(FULL_MASK, acc.hi, m);
-    o.lo = __shfl_xor_sync(FULL_MASK, acc.lo, m);
-    acc = cf_add2(acc, o);
-  }
-  if (lane == 0) {
-    // in FP32: the sum is exact to ~1e-12 and the output is a float (an FP64
-    // division and square root are long FP64 sequences on GB300)
-    float msd = __fadd_rn(acc.hi, acc.lo) * (1.0f / (float)A);
-    if (!(msd > 0.0f)) msd = 0.0f;
-    r.out_rmsd[en.frame] = sqrtf(msd);
-  }
 }
 
 // Refinement of a queue filled by finish_kernel: one warp per entry.
@@ -635,9 +777,17 @@ constexpr StreamCfg kCfgs[kNumCfg] = {
 };
 int g_forced_cfg = -1;
 
-size_t stream_smem_bytes(const StreamCfg& c, int32_t Ap, bool use_ref) {
+size_t stream_smem_bytes(const StreamCfg& c, int32_t Ap, bool use_ref, bool fin = false) {
   const size_t ref = (c.ref_smem && use_ref) ? align_up((size_t)Ap * 12, 128) : 0;
-  return ref + (size_t)c.warps * c.nstage * c.cq * 48 + (size_t)c.warps * c.nstage * 8;
+  const size_t fin_state = fin ? 16 : 0;  // the in-kernel finish's refinement count
+  return ref + (size_t)c.warps * c.nstage * c.cq * 48 + (size_t)c.warps * c.nstage * 8 + fin_state;
+}
+
+// The in-kernel finish is built for the 16-warp configurations of the
+// single-reference RMSD modes with one unit per frame.
+bool fin_usable(const StreamCfg& c, int mode, int32_t S, int32_t Ap) {
+  return S == 1 && c.warps == 16 && (mode == MODE_CENTER || mode == MODE_PRECENTERED) &&
+         stream_smem_bytes(c, Ap, true, true) <= (size_t)max_dyn_smem();
 }
 
 bool cfg_fits(const StreamCfg& c, int32_t Ap, bool use_ref) {
@@ -689,41 +839,53 @@ int32_t choose_splits(int64_t F, int32_t Q, int gwarps) {
   return best_s;
 }
 
-template <int LAYOUT, int MODE, int CQ, int NSTAGE, bool REF_SMEM, int WARPS>
-int launch_stream_t(const StreamArgs& a, const CUtensorMap& tmap, size_t smem, int grid, cudaStream_t st) {
-  auto k = stream_kernel<LAYOUT, MODE, CQ, NSTAGE, REF_SMEM, WARPS>;
+template <int LAYOUT, int MODE, int CQ, int NSTAGE, bool REF_SMEM, int WARPS, bool FIN>
+int launch_stream_t(const StreamArgs& a, const CUtensorMap& tmap, const FinishArgs& fa, const RefineArgs& ra,
+                    size_t smem, int grid, cudaStream_t st) {
+  auto k = stream_kernel<LAYOUT, MODE, CQ, NSTAGE, REF_SMEM, WARPS, FIN>;
   GB_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
               "cudaFuncSetAttribute(stream_kernel)");
-  k<<<grid, WARPS * 32, smem, st>>>(a, tmap);
+  k<<<grid, WARPS * 32, smem, st>>>(a, tmap, fa, ra);
   GB_CUDA_TRY(cudaGetLastError(), "launch stream_kernel");
   return GBRMSD_OK;
 }
 
 template <int LAYOUT, int MODE>
-int launch_stream_m(const StreamArgs& a, const CUtensorMap& tm, const StreamCfg& c, size_t smem, int grid,
-                    cudaStream_t st) {
-#define GB_CFG(W, CQ_, NS, RS)                                                  \
-  if (c.warps == W && c.cq == CQ_ && c.nstage == NS && c.ref_smem == RS)       \
-    return launch_stream_t<LAYOUT, MODE, CQ_, NS, RS, W>(a, tm, smem, grid, st);
-  GB_CFG(16, 128, 2, true)
-  GB_CFG(16, 64, 3, true)
-  GB_CFG(16, 64, 2, true)
-  GB_CFG(16, 64, 4, false)
-  GB_CFG(8, 128, 3, true)
-  GB_CFG(8, 64, 4, true)
-  GB_CFG(8, 128, 4, false)
+int launch_stream_m(const StreamArgs& a, const CUtensorMap& tm, const StreamCfg& c, const FinishArgs* fin,
+                    const RefineArgs* rfin, size_t smem, int grid, cudaStream_t st) {
+  const FinishArgs fa = fin ? *fin : FinishArgs{};
+  const RefineArgs ra = rfin ? *rfin : RefineArgs{};
+#define GB_CFG(W, CQ_, NS, RS, FIN_)                                                            \
+  if (c.warps == W && c.cq == CQ_ && c.nstage == NS && c.ref_smem == RS)                       \
+    return launch_stream_t<LAYOUT, MODE, CQ_, NS, RS, W, FIN_>(a, tm, fa, ra, smem, grid, st);
+  if constexpr (MODE == MODE_CENTER || MODE == MODE_PRECENTERED) {
+    if (fin) {
+      GB_CFG(16, 128, 2, true, true)
+      GB_CFG(16, 64, 3, true, true)
+      GB_CFG(16, 64, 2, true, true)
+      GB_CFG(16, 64, 4, false, true)
+      return set_error(GBRMSD_E_INVALID, "no in-kernel finish for this configuration");
+    }
+  }
+  GB_CFG(16, 128, 2, true, false)
+  GB_CFG(16, 64, 3, true, false)
+  GB_CFG(16, 64, 2, true, false)
+  GB_CFG(16, 64, 4, false, false)
+  GB_CFG(8, 128, 3, true, false)
+  GB_CFG(8, 64, 4, true, false)
+  GB_CFG(8, 128, 4, false, false)
 #undef GB_CFG
   return set_error(GBRMSD_E_INVALID, "no streaming kernel for this configuration");
 }
 
 template <int LAYOUT>
-int launch_stream_l(int mode, const StreamArgs& a, const CUtensorMap& tm, const StreamCfg& c, size_t smem,
-                    int grid, cudaStream_t st) {
+int launch_stream_l(int mode, const StreamArgs& a, const CUtensorMap& tm, const StreamCfg& c,
+                    const FinishArgs* fin, const RefineArgs* rfin, size_t smem, int grid, cudaStream_t st) {
   switch (mode) {
-    case MODE_CENTER: return launch_stream_m<LAYOUT, MODE_CENTER>(a, tm, c, smem, grid, st);
-    case MODE_PRECENTERED: return launch_stream_m<LAYOUT, MODE_PRECENTERED>(a, tm, c, smem, grid, st);
-    case MODE_NOSUPERPOSE: return launch_stream_m<LAYOUT, MODE_NOSUPERPOSE>(a, tm, c, smem, grid, st);
-    default: return launch_stream_m<LAYOUT, MODE_TRACE>(a, tm, c, smem, grid, st);
+    case MODE_CENTER: return launch_stream_m<LAYOUT, MODE_CENTER>(a, tm, c, fin, rfin, smem, grid, st);
+    case MODE_PRECENTERED: return launch_stream_m<LAYOUT, MODE_PRECENTERED>(a, tm, c, fin, rfin, smem, grid, st);
+    case MODE_NOSUPERPOSE: return launch_stream_m<LAYOUT, MODE_NOSUPERPOSE>(a, tm, c, nullptr, nullptr, smem, grid, st);
+    default: return launch_stream_m<LAYOUT, MODE_TRACE>(a, tm, c, nullptr, nullptr, smem, grid, st);
   }
 }
 
@@ -759,21 +921,24 @@ int encode_axis_map(CUtensorMap* tm, const StreamArgs& a) {
   return GBRMSD_OK;
 }
 
-int launch_stream(int layout, int mode, const StreamArgs& args, const StreamCfg& c, cudaStream_t st) {
+// fin / rfin non-null: the call's finish runs inside the streaming kernel
+// (fin_usable must hold); otherwise the caller launches the finish.
+int launch_stream(int layout, int mode, const StreamArgs& args, const StreamCfg& c, cudaStream_t st,
+                  const FinishArgs* fin = nullptr, const RefineArgs* rfin = nullptr) {
   StreamArgs a = args;
   a.wait_ns = wait_limit_ns();
   a.skip_unit = skip_unit_hook();
   const bool use_ref = mode != MODE_TRACE;
-  const size_t smem = stream_smem_bytes(c, a.n_padded, use_ref);
+  const size_t smem = stream_smem_bytes(c, a.n_padded, use_ref, fin != nullptr);
   const int grid = sm_count();
   alignas(64) CUtensorMap tm;
   memset(&tm, 0, sizeof(tm));
   if (layout == AXIS_MAJOR) {
     const int rc = encode_axis_map(&tm, a);
     if (rc) return rc;
-    return launch_stream_l<AXIS_MAJOR>(mode, a, tm, c, smem, grid, st);
+    return launch_stream_l<AXIS_MAJOR>(mode, a, tm, c, fin, rfin, smem, grid, st);
   }
-  return launch_stream_l<ATOM_MAJOR>(mode, a, tm, c, smem, grid, st);
+  return launch_stream_l<ATOM_MAJOR>(mode, a, tm, c, fin, rfin, smem, grid, st);
 }
 
 struct WsLayout {
@@ -985,10 +1150,6 @@ int gbrmsd_rmsd_to_reference(const float* x, int64_t n_frames, int32_t n_atoms, 
   sa.splits = S;
   sa.sums = reinterpret_cast<double*>(w + L.sums_off);
   sa.err = &hdr->err;
-  prof_begin(st);
-  rc = launch_stream(layout, mode, sa, cfg, st);
-  if (rc) return rc;
-  prof_end(st);
 
   FinishArgs fa;
   fa.n_frames = n_frames;
@@ -1021,6 +1182,18 @@ int gbrmsd_rmsd_to_reference(const float* x, int64_t n_frames, int32_t n_atoms, 
   ra.count = fa.refine_count;
   ra.out_rmsd = out_rmsd;
   ra.out_centroid = out_centroid;
+
+  // One launch when every frame is one unit: each CTA solves its own
+  // frames at the end of the streaming kernel (no second kernel).
+  fa.inv_hi = (float)fa.inv_atoms;
+  fa.inv_lo = (float)(fa.inv_atoms - (double)fa.inv_hi);
+  const bool fin = fin_usable(cfg, mode, S, n_padded);
+  prof_begin(st);
+  rc = fin ? launch_stream(layout, mode, sa, cfg, st, &fa, &ra) : launch_stream(layout, mode, sa, cfg, st);
+  if (rc) return rc;
+  prof_end(st);
+  if (fin) return GBRMSD_OK;
+
   // equal shares of at most 128 frames per block, one block per SM while
   // they fit
   const int64_t sms = sm_count();

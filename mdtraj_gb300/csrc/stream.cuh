@@ -27,6 +27,8 @@ struct RefInfo {
   int32_t n_padded;
   int32_t layout;
   int32_t centred;
+  float g_hi, g_lo;          // g and sum as float pairs (hi + lo), for
+  float sum_hi[3], sum_lo[3];  // finishes that use no FP64
 };
 
 // A frame whose QCP msd is too small for the one-pass sums to resolve; the
@@ -78,6 +80,7 @@ struct FinishArgs {
   int32_t mode;
   float* out_rot;             // optional, n_frames x 9 (superposition)
   double* out_mu;             // optional with out_rot, n_frames x 3
+  float inv_hi, inv_lo;       // 1 / n_atoms as a float pair (in-kernel finish)
 };
 
 }  // namespace gb

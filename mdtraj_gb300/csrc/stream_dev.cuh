@@ -110,8 +110,12 @@ __device__ __forceinline__ void prepare_reference_block(const float* __restrict_
     for (int c = 0; c < 3; ++c) prefix[c] = 0.0;
   if (tid == 0) {
     info->g = g;
+    info->g_hi = (float)g;
+    info->g_lo = (float)(g - (double)info->g_hi);
     for (int c = 0; c < 3; ++c) {
       info->sum[c] = sb[c];
+      info->sum_hi[c] = (float)sb[c];
+      info->sum_lo[c] = (float)(sb[c] - (double)info->sum_hi[c]);
       info->centroid[c] = mu[c];
     }
     info->n_atoms = A;
@@ -244,6 +248,10 @@ struct FrameCtx {
   double* out_mu;          // optional with out_rot: FP64 centroid per frame, 3 doubles
 };
 
+// Split records are read through L2 (ld.global.cg): the streaming kernel's
+// in-kernel finish reads records other warps of its CTA have just written.
+__device__ __forceinline__ double ldrec(const double* p) { return __ldcg(p); }
+
 // A frame that needs the refinement pass is queued in refine[] (refine_count
 // the queue's length), or, when `held` is given, handed back in *held with
 // *pending set, for the caller to refine at once.
@@ -259,7 +267,7 @@ __device__ __forceinline__ void finish_frame(const FrameCtx& c, float* out_rmsd,
 
   if (c.mode == MODE_NOSUPERPOSE) {
     double g = 0.0;
-    for (int j = 0; j < S; ++j) g += base[j * SUMS_STRIDE + 12];
+    for (int j = 0; j < S; ++j) g += ldrec(base + j * SUMS_STRIDE + 12);
     double msd = g * invA;
     if (!(msd > 0.0)) msd = 0.0;
     out_rmsd[f] = (float)sqrt(msd);
@@ -268,7 +276,7 @@ __device__ __forceinline__ void finish_frame(const FrameCtx& c, float* out_rmsd,
   if (c.mode == MODE_TRACE) {
     for (int k = 0; k < 3; ++k) {
       double s = 0.0;
-      for (int j = 0; j < S; ++j) s += base[j * SUMS_STRIDE + 9 + k];
+      for (int j = 0; j < S; ++j) s += ldrec(base + j * SUMS_STRIDE + 9 + k);
       out_centroid[3 * f + k] = (float)(s * invA);
     }
     return;
@@ -278,7 +286,7 @@ __device__ __forceinline__ void finish_frame(const FrameCtx& c, float* out_rmsd,
   double ga, gb, mu[3] = {0.0, 0.0, 0.0};
   if (c.mode == MODE_PRECENTERED) {
     for (int j = 0; j < S; ++j)
-      for (int i = 0; i < 9; ++i) m[i] += base[j * SUMS_STRIDE + i];
+      for (int i = 0; i < 9; ++i) m[i] += ldrec(base + j * SUMS_STRIDE + i);
     ga = (double)c.g_target;
     gb = (double)c.g_ref;
   } else {
@@ -287,7 +295,7 @@ __device__ __forceinline__ void finish_frame(const FrameCtx& c, float* out_rmsd,
       const double* r = base + j * SUMS_STRIDE;
       const int32_t q0 = (int32_t)(((int64_t)j * Q) / S), q1 = (int32_t)(((int64_t)(j + 1) * Q) / S);
       const double nj = (double)(min(4 * q1, A) - 4 * q0);
-      for (int k = 0; k < 3; ++k) sa[k] += r[9 + k] + nj * r[16 + k];
+      for (int k = 0; k < 3; ++k) sa[k] += ldrec(r + 9 + k) + nj * ldrec(r + 16 + k);
     }
     for (int k = 0; k < 3; ++k) mu[k] = sa[k] * invA;
     ga = 0.0;
@@ -297,13 +305,13 @@ __device__ __forceinline__ void finish_frame(const FrameCtx& c, float* out_rmsd,
       const double nj = (double)(min(4 * q1, A) - 4 * q0);
       double ds[3], bj[3];
       for (int k = 0; k < 3; ++k) {
-        ds[k] = r[16 + k] - mu[k];
+        ds[k] = ldrec(r + 16 + k) - mu[k];
         bj[k] = c.ref_prefix[3 * (size_t)q1 + k] - c.ref_prefix[3 * (size_t)q0 + k];
       }
-      ga += r[12] + 2.0 * (ds[0] * r[9] + ds[1] * r[10] + ds[2] * r[11]) +
+      ga += ldrec(r + 12) + 2.0 * (ds[0] * ldrec(r + 9) + ds[1] * ldrec(r + 10) + ds[2] * ldrec(r + 11)) +
             nj * (ds[0] * ds[0] + ds[1] * ds[1] + ds[2] * ds[2]);
       for (int i = 0; i < 3; ++i)
-        for (int k = 0; k < 3; ++k) m[3 * i + k] += r[3 * i + k] + ds[i] * bj[k];
+        for (int k = 0; k < 3; ++k) m[3 * i + k] += ldrec(r + 3 * i + k) + ds[i] * bj[k];
     }
     gb = c.ref_info->g;
     if (out_centroid)
@@ -381,6 +389,109 @@ __device__ __forceinline__ void finish_frame(const FrameCtx& c, float* out_rmsd,
     } else {
       refine[atomicAdd(refine_count, 1)] = e;
     }
+  }
+}
+
+// Records of the in-kernel finish (one unit per frame) hold float pairs in
+// the unit's SUMS_STRIDE slot: sum j as (hi, lo) at floats [2j, 2j + 1]
+// (j < 13: M, then MODE_CENTER's coordinate sum and trace about the shift),
+// MODE_CENTER's float shift at [DFREC_SHIFT, +3).
+constexpr int DFREC_SHIFT = 26;
+
+// finish_frame for such a record, with no FP64 instruction on the common
+// path (GB300 issues one FP64 instruction per ~64 cycles of a sub-partition;
+// the FP64 recombination and conversions were half of finish_frame's
+// latency): the re-centring of a whole frame, with s the shift, sd = sum (a - s)
+// and sdA = sd / A,
+//   mu = s + sdA,  Ga = g - sdA . sd,  M = m - sdA (sum_k b_k)^T,
+// runs in float pairs and feeds qcp_lambda_max_dfm directly.  FP64 remains
+// for the double-root polish and for building a refinement entry (rare).
+__device__ __forceinline__ void finish_frame_df(const float* rec, int64_t f, const FinishArgs& a, DF inv,
+                                                RefineEntry* held, bool* pending) {
+  const int32_t A = a.n_atoms;
+  const RefInfo* ri = a.ref_info;
+  DF m[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) m[i] = DF{__ldcg(rec + 2 * i), __ldcg(rec + 2 * i + 1)};
+  DF ga, gb, mu[3] = {DF{0.f, 0.f}, DF{0.f, 0.f}, DF{0.f, 0.f}};
+  if (a.mode == MODE_PRECENTERED) {
+    ga = DF{a.g_target[f], 0.f};
+    gb = DF{a.g_ref_override, 0.f};
+  } else {
+    DF sd[3], sdA[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      sd[k] = DF{__ldcg(rec + 18 + 2 * k), __ldcg(rec + 19 + 2 * k)};
+      sdA[k] = df_mul(sd[k], inv);
+      mu[k] = df_add_f(sdA[k], __ldcg(rec + DFREC_SHIFT + k));
+    }
+    const DF g = DF{__ldcg(rec + 24), __ldcg(rec + 25)};
+    ga = df_sub(g, df_add(df_add(df_mul(sdA[0], sd[0]), df_mul(sdA[1], sd[1])), df_mul(sdA[2], sd[2])));
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const DF bs = DF{ri->sum_hi[k], ri->sum_lo[k]};
+#pragma unroll
+      for (int i = 0; i < 3; ++i) m[3 * i + k] = df_sub(m[3 * i + k], df_mul(sdA[i], bs));
+    }
+    gb = DF{ri->g_hi, ri->g_lo};
+    if (a.out_centroid)
+      for (int k = 0; k < 3; ++k) a.out_centroid[3 * f + k] = __fadd_rn(mu[k].hi, mu[k].lo);
+    if (a.out_trace) a.out_trace[f] = __fadd_rn(ga.hi, ga.lo);
+  }
+  bool self = (f == a.self_index);
+  if (self && a.mode == MODE_PRECENTERED) self = (a.g_target[f] == a.g_ref_override);
+  if (self) {
+    a.out_rmsd[f] = 0.f;
+    return;
+  }
+  bool finite = isfinite(ga.hi) && isfinite(ga.lo) && isfinite(gb.hi) && isfinite(gb.lo);
+#pragma unroll
+  for (int i = 0; i < 9; ++i) finite = finite && isfinite(m[i].hi) && isfinite(m[i].lo);
+  if (!finite) {
+    // as finish_frame: the reference's clamp of a NaN msd gives 0, and the
+    // centroid is recomputed by plain FP64 sums in the refinement pass
+    atomicOr(a.err, DEV_ERR_NONFINITE);
+    a.out_rmsd[f] = 0.f;
+    if (a.out_centroid && a.mode == MODE_CENTER) {
+      RefineEntry e;
+      e.frame = f;
+      for (int i = 0; i < 9; ++i) e.rot[i] = 0.f;
+      for (int k = 0; k < 3; ++k) { e.mu_hi[k] = 0.f; e.mu_lo[k] = 0.f; }
+      e.seg = -1;
+      *held = e;
+      *pending = true;
+    }
+    return;
+  }
+  int iters = 0;
+  bool short_ = false;
+  DF lam = qcp_lambda_max_dfm(m, df_mul_f(df_add(ga, gb), 0.5f), &iters, &short_);
+  if (short_) {  // (near) double root: rare, FP64
+    double md[9];
+    for (int i = 0; i < 9; ++i) md[i] = df_to_double(m[i]);
+    lam = df_from_double(qcp_newton_fp64(md, df_to_double(lam)));
+  }
+  const DF t = df_sub(df_add(ga, gb), df_mul_f(lam, 2.0f));
+  const DF msd_df = df_mul(t, inv);
+  float msd = __fadd_rn(msd_df.hi, msd_df.lo);
+  if (!(msd > 0.0f)) msd = 0.0f;
+  a.out_rmsd[f] = sqrtf(msd);
+  // One-pass sums resolve msd to about 1e-7 * scale / sqrt(A); below
+  // (0.1 * scale / sqrt(A))^2 the direct residual is recomputed.
+  const float scale = __fmul_rn(__fadd_rn(ga.hi, gb.hi), 0.5f * inv.hi);
+  if (msd * (float)A < 0.01f * scale * scale && A > 0) {
+    RefineEntry e;
+    double md[9];
+    for (int i = 0; i < 9; ++i) md[i] = df_to_double(m[i]);
+    qcp_rotation_refine(md, df_to_double(lam), e.rot);
+    e.frame = f;
+    for (int k = 0; k < 3; ++k) {
+      e.mu_hi[k] = mu[k].hi;
+      e.mu_lo[k] = mu[k].lo;
+    }
+    e.seg = 0;
+    *held = e;
+    *pending = true;
   }
 }
 

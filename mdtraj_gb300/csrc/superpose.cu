@@ -13,9 +13,12 @@
 //                           (rot_msd_atom_major, src/rotation_generic.h:47-103,
 //                           as used by getMultipleAlignDisplaceRMSDs_atom_major,
 //                           _rmsd.pyx:677-759)
+//   center_weighted_kernel  warp per frame: x <- x - sum_k w_k x_k in place
+//                           (Trajectory.center_coordinates(mass_weighted=True),
+//                           mdtraj/core/trajectory.py:2133-2134)
 //
 // Rotations come from gbrmsd_rotations (row-major R, aligned = R x).  All
-// three kernels are HBM-bound streaming passes over float32 coordinates.
+// four kernels are HBM-bound streaming passes over float32 coordinates.
 #include <math.h>
 #include <string.h>
 
@@ -267,6 +270,94 @@ __global__ void __launch_bounds__(256) rotated_msd_kernel(const float* __restric
   }
 }
 
+// ---------------------------------------------------------------------------
+// Mass-weighted centring (Trajectory.center_coordinates(mass_weighted=True))
+// ---------------------------------------------------------------------------
+
+constexpr int CW_THREADS = 256;  // 8 warps: one frame each per round
+constexpr int CW_CHUNK = 2048;   // weights staged per round as float pairs (16 KB)
+
+// x_f <- x_f - com_f in place, com_f = sum_k w_k x_fk with the caller's
+// (normalised) weights, one warp per frame.  The reference forms com in FP64
+// (mdtraj/geometry/distance.py:366-384, x.astype(float64).T.dot(masses)) and
+// subtracts it from the float32 coordinates through numpy's float64 loop
+// (mdtraj/core/trajectory.py:2133-2134), i.e. x <- float(double(x) - com).
+// Here the weights are split into float pairs (hi + lo) once per CTA round,
+// products w x are formed error-free in FP32 (FMA residual), summed in
+// float pairs (~48 bits), and the subtraction float(x - (ch + cl)) is taken
+// through TwoSum: the same float as the FP64 form except where x - com lies
+// within ~2^-40 of a rounding midpoint.  No FP64 per atom (GB300's FP64
+// pipe is narrow).  Pass 2 re-reads the frame, which a warp has just read
+// (L1/L2).
+__global__ void __launch_bounds__(CW_THREADS) center_weighted_kernel(float* __restrict__ x, int64_t F, int32_t A,
+                                                                    int64_t fs, const double* __restrict__ w,
+                                                                    double* __restrict__ com_out) {
+  __shared__ float2 sw[CW_CHUNK];
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  constexpr int WPB = CW_THREADS / 32;
+  const int64_t rounds = (F + WPB - 1) / WPB;
+  for (int64_t b = blockIdx.x; b < rounds; b += gridDim.x) {
+    const int64_t f = b * WPB + warp;
+    const bool live = f < F;
+    float* fr = x + (live ? f : 0) * fs;
+    CF s[3] = {cf_zero(), cf_zero(), cf_zero()};
+    for (int32_t k0 = 0; k0 < A; k0 += CW_CHUNK) {
+      const int n = min(CW_CHUNK, A - k0);
+      __syncthreads();  // the previous chunk's weights are no longer read
+      for (int i = threadIdx.x; i < n; i += CW_THREADS) {
+        const double d = w[k0 + i];
+        const float hi = (float)d;
+        sw[i] = make_float2(hi, (float)(d - (double)hi));
+      }
+      __syncthreads();
+      if (live) {
+        for (int i = lane; i < n; i += 32) {
+          const float2 ww = sw[i];
+          const float* p = fr + 3 * (size_t)(k0 + i);
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            const float v = p[c];
+            const float ph = __fmul_rn(ww.x, v);  // not contracted into the sums below
+            float pl = fmaf(ww.y, v, fmaf(ww.x, v, -ph));  // w x - ph to ~2^-48
+            if (!isfinite(ph)) pl = 0.f;  // inf - inf: an infinite product carries no low part
+            cf_add(s[c], ph);
+            cf_add(s[c], pl);
+          }
+        }
+      }
+    }
+    if (!live) continue;
+    float ch[3], cl[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      CF v = s[c];
+#pragma unroll
+      for (int m = 16; m >= 1; m >>= 1) {
+        CF o;
+        o.hi = __shfl_xor_sync(FULL_MASK, v.hi, m);
+        o.lo = __shfl_xor_sync(FULL_MASK, v.lo, m);
+        v = cf_add2(v, o);
+      }
+      ch[c] = v.hi;
+      cl[c] = isfinite(v.hi) ? v.lo : 0.f;  // an infinite com carries no low part
+    }
+    if (lane == 0 && com_out)
+      for (int c = 0; c < 3; ++c) com_out[3 * f + c] = (double)ch[c] + (double)cl[c];
+    __syncwarp();
+    for (int32_t k = lane; k < A; k += 32) {
+      float* p = fr + 3 * (size_t)k;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const float v = p[c];
+        float sh, sl;
+        two_sum(v, -ch[c], sh, sl);  // v - ch exactly
+        p[c] = isfinite(ch[c]) ? __fadd_rn(sh, __fsub_rn(sl, cl[c])) : __fsub_rn(v, ch[c]);
+      }
+    }
+  }
+}
+
 int check_rows(const void* x, int64_t F, int32_t A, int64_t fs, const char* who) {
   if (F < 0 || A < 0) return set_error(GBRMSD_E_INVALID, "%s: negative sizes", who);
   if (fs < 3LL * A) return set_error(GBRMSD_E_INVALID, "%s: frame_stride must be >= 3 * n_atoms", who);
@@ -354,6 +445,29 @@ int gbrmsd_rotated_rmsd(const float* x, int64_t n_frames, int32_t n_atoms, int64
   rotated_msd_kernel<<<(unsigned)(blocks > 0 ? blocks : 1), 256, 0, st>>>(x, n_frames, n_atoms, frame_stride, rot,
                                                                           ref_frame, out_rmsd);
   GB_CUDA_TRY(cudaGetLastError(), "launch rotated_msd_kernel");
+  return GBRMSD_OK;
+}
+
+int gbrmsd_center_weighted_inplace(float* x, int64_t n_frames, int32_t n_atoms, int64_t frame_stride,
+                                   const double* weights, double* out_com, void* stream) {
+  clear_error();
+  int rc = check_rows(x, n_frames, n_atoms, frame_stride, "center_weighted_inplace");
+  if (rc) return rc;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (n_frames == 0) return GBRMSD_OK;
+  if (n_atoms == 0) {
+    // the reference's dot product over no atoms is 0: nothing moves
+    if (out_com) GB_CUDA_TRY(cudaMemsetAsync(out_com, 0, sizeof(double) * 3 * n_frames, st), "memset com");
+    return GBRMSD_OK;
+  }
+  if (!weights) return set_error(GBRMSD_E_INVALID, "center_weighted_inplace: null weights");
+  const int64_t rounds = (n_frames + CW_THREADS / 32 - 1) / (CW_THREADS / 32);
+  const int64_t blocks = std::min<int64_t>(rounds, (int64_t)sm_count() * 8);
+  prof_begin(st);
+  center_weighted_kernel<<<(unsigned)blocks, CW_THREADS, 0, st>>>(x, n_frames, n_atoms, frame_stride, weights,
+                                                                  out_com);
+  GB_CUDA_TRY(cudaGetLastError(), "launch center_weighted_kernel");
+  prof_end(st);
   return GBRMSD_OK;
 }
 

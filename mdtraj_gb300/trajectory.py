@@ -3,7 +3,7 @@ mdtraj.Trajectory (mdtraj/core/trajectory.py): float32 C-contiguous ``xyz``
 whose setter drops cached traces (:1010-1029), ``_rmsd_traces`` filled by
 ``center_coordinates`` (:2114-2137) and carried through frame slicing
 (:1325-1361).  Topology handling is out of scope; ``topology`` is stored
-as given."""
+as given and only read for the atom masses of mass-weighted centring."""
 from __future__ import annotations
 
 import numpy as np
@@ -62,14 +62,22 @@ class Trajectory:
         return out
 
     def center_coordinates(self, mass_weighted=False):
-        """Centres each frame at the origin in place and caches the traces
-        used by ``rmsd(..., precentered=True)``.  Mass weighting needs a
-        topology with masses and is not supported by this container."""
-        from ._rmsd import _center_inplace_atom_major
+        """Centres each frame at the origin in place
+        (core/trajectory.py:2114-2137).  Uniform weights cache the traces
+        used by ``rmsd(..., precentered=True)``; with ``mass_weighted`` and a
+        topology, each frame's centre of mass (masses ``atom.element.mass``
+        of ``topology.atoms``, normalised to sum 1) is subtracted instead and
+        the cached traces are dropped, as the reference's assignment to
+        ``xyz`` drops them."""
+        from ._rmsd import _center_inplace_atom_major, _center_weighted_inplace_atom_major
 
         if mass_weighted and self.topology is not None:
-            raise NotImplementedError("mass-weighted centring needs atom masses from a topology")
-        self._rmsd_traces = _center_inplace_atom_major(self._xyz)
+            masses = np.array([a.element.mass for a in self.topology.atoms])
+            masses /= masses.sum()
+            _center_weighted_inplace_atom_major(self._xyz, masses)
+            self.xyz = self._xyz
+        else:
+            self._rmsd_traces = _center_inplace_atom_major(self._xyz)
         return self
 
     def superpose(self, reference, frame=0, atom_indices=None, ref_atom_indices=None, parallel=True):

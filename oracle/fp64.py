@@ -127,3 +127,20 @@ def align_displace(align_ref: np.ndarray, align: np.ndarray, displ_ref: np.ndarr
     d = np.einsum("fij,fkj->fki", R, np.asarray(displ, dtype=np.float64)) - np.asarray(displ_ref, dtype=np.float64)
     n = max(displ.shape[1], 1)
     return np.sqrt((d * d).sum((1, 2)) / n), R
+
+
+def center_of_mass_inplace(xyz: np.ndarray, masses: np.ndarray) -> np.ndarray:
+    """Trajectory.center_coordinates(mass_weighted=True) restated: masses
+    normalised to sum 1 (mdtraj/geometry/distance.py:369-370), each frame's
+    centre of mass as a float64 dot product (:382-384), subtracted from the
+    float32 coordinates through numpy's float64 loop
+    (mdtraj/core/trajectory.py:2133-2134).  Modifies `xyz` in place and
+    returns the (F, 3) centres."""
+    w = np.array(masses, dtype=np.float64)
+    w /= w.sum()
+    com = np.empty((xyz.shape[0], 3))
+    for i, x in enumerate(xyz):
+        com[i, :] = x.astype("float64").T.dot(w)
+    with np.errstate(invalid="ignore"):
+        xyz -= com[:, np.newaxis, :]
+    return com

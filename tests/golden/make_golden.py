@@ -28,8 +28,11 @@ through a stub ``mdtraj`` package, and records:
 * xtc_{water,tiny,wide}.xtc + xtc_cases.npz — synthetic trajectories written
                     by the reference's XTC writer, with its reader's output
                     (coordinates, time, step, box) for the GPU decoder.
+* center_mass.npz — Trajectory.center_coordinates(mass_weighted=True), run
+                    from the reference's own source of that method and of
+                    compute_center_of_mass.
 
-Usage:  MDTRAJ_REF=<reference checkout> python tests/golden/make_golden.py
+Usage:  MDTRAJ_REF=<reference checkout> python tests/golden/make_golden.py [fixture ...]
 """
 from __future__ import annotations
 
@@ -335,17 +338,112 @@ def xtc_fixture(xtc) -> None:
     np.savez_compressed(OUT / "xtc_cases.npz", **arrays)
 
 
-def main() -> None:
+def _reference_function(path: Path, name: str, cls: str | None = None):
+    """Source of one function (or method of class `cls`) of a reference
+    module, parsed with ast (core/ and geometry/ import compiled modules that
+    are not built here, so the module itself cannot be imported)."""
+    tree = ast.parse(path.read_text())
+    body = tree.body
+    if cls is not None:
+        body = next(n for n in body if isinstance(n, ast.ClassDef) and n.name == cls).body
+    node = next(n for n in body if isinstance(n, ast.FunctionDef) and n.name == name)
+    node.decorator_list = []
+    return ast.unparse(node)
+
+
+def center_mass_fixture() -> None:
+    """center_mass.npz: Trajectory.center_coordinates(mass_weighted=True) of
+    the reference (core/trajectory.py:2114-2137 with
+    geometry/distance.py:349-384, both run from their own source) on
+    duck-typed trajectories whose atoms carry element masses.  Cases: 'mixed'
+    (H/C/N/O/S masses), 'chunk' (2,101 atoms), 'hydrogen' (equal masses, the
+    reference's test_center), 'nonfinite' (an inf and a NaN coordinate)."""
+    ns = {"np": np}
+    exec(_reference_function(REF / "mdtraj" / "geometry" / "distance.py", "compute_center_of_mass"), ns)
+    meth = {"np": np, "distance": types.SimpleNamespace(compute_center_of_mass=ns["compute_center_of_mass"])}
+    exec(_reference_function(REF / "mdtraj" / "core" / "trajectory.py", "center_coordinates", "Trajectory"), meth)
+
+    class Atom:
+        def __init__(self, mass):
+            self.element = types.SimpleNamespace(mass=float(mass))
+
+    class Top:
+        def __init__(self, masses):
+            self._atoms = [Atom(m) for m in masses]
+
+        @property
+        def atoms(self):
+            return iter(self._atoms)
+
+    class T:
+        def __init__(self, xyz, masses):
+            self.top = self.topology = Top(masses)
+            self._xyz = xyz
+            self._rmsd_traces = np.zeros(len(xyz), np.float32)
+
+        @property
+        def xyz(self):
+            return self._xyz
+
+        @xyz.setter
+        def xyz(self, v):  # the reference setter's effect on these arrays (core/trajectory.py:1010-1029)
+            self._xyz = np.asarray(v, dtype=np.float32)
+            self._rmsd_traces = None
+
+        @property
+        def n_frames(self):
+            return len(self._xyz)
+
+    rng = np.random.default_rng(77)
+    table = np.array([1.008, 12.011, 14.007, 15.999, 32.06])
+    cases = {
+        "mixed": (rng.uniform(-3, 5, size=(7, 23, 3)), table[rng.integers(0, 5, 23)]),
+        "chunk": (rng.uniform(-1, 9, size=(3, 2101, 3)) + 40.0, table[rng.integers(0, 5, 2101)]),
+        "hydrogen": (rng.normal(1.5, 2.0, size=(5, 37, 3)), np.full(37, 1.008)),
+    }
+    bad = rng.uniform(-2, 2, size=(3, 5, 3))
+    bad[1, 2, 0] = np.inf
+    bad[2, 4, 1] = np.nan
+    cases["nonfinite"] = (bad, table[rng.integers(0, 5, 5)])
+    arrays = {}
+    for name, (x, masses) in cases.items():
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        t = T(x.copy(), masses)
+        with np.errstate(invalid="ignore"):
+            meth["center_coordinates"](t, mass_weighted=True)
+        assert t._rmsd_traces is None
+        arrays[f"{name}__xyz"] = x
+        arrays[f"{name}__masses"] = masses
+        arrays[f"{name}__centred"] = t.xyz
+    np.savez_compressed(OUT / "center_mass.npz", **arrays)
+
+
+FIXTURES = ("frame0", "alignment", "synthetic", "superpose", "xtc", "center_mass")
+
+
+def main(only: list[str]) -> None:
+    """Writes every fixture, or only those named on the command line."""
+    want = set(only or FIXTURES)
+    unknown = want - set(FIXTURES)
+    if unknown:
+        sys.exit(f"make_golden.py: unknown fixtures {sorted(unknown)}; choose from {FIXTURES}")
     build_reference_python()
     _rmsd, xtc = import_reference()
-    frame0_fixture(_rmsd, xtc)
-    alignment_fixture()
-    synthetic_fixture(_rmsd)
-    superpose_fixture(_rmsd)
-    xtc_fixture(xtc)
+    if "frame0" in want:
+        frame0_fixture(_rmsd, xtc)
+    if "alignment" in want:
+        alignment_fixture()
+    if "synthetic" in want:
+        synthetic_fixture(_rmsd)
+    if "superpose" in want:
+        superpose_fixture(_rmsd)
+    if "xtc" in want:
+        xtc_fixture(xtc)
+    if "center_mass" in want:
+        center_mass_fixture()
     for p in sorted(OUT.glob("*.npz")):
         print(p.name, p.stat().st_size, "bytes")
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

@@ -191,3 +191,14 @@ def test_port_restates_the_reference_on_degenerate_structures(shape):
     else:
         np.testing.assert_allclose(a[~copies], b[~copies], atol=2e-5, err_msg=shape)
         assert ea.max() <= ABS_TOL and eb.max() <= ABS_TOL, (shape, ea.max(), eb.max())
+
+
+def test_fp64_center_of_mass_matches_reference(golden):
+    """The mass-weighted centring restatement reproduces the reference's own
+    center_coordinates(mass_weighted=True) bit for bit (non-finite frames
+    included)."""
+    d = golden("center_mass.npz")
+    for name in ("mixed", "chunk", "hydrogen", "nonfinite"):
+        x = d[f"{name}__xyz"].copy()
+        fp64.center_of_mass_inplace(x, d[f"{name}__masses"])
+        np.testing.assert_array_equal(x, d[f"{name}__centred"], err_msg=name)
