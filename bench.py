@@ -557,11 +557,16 @@ def run_e2e(args, F, A, s_lo, s_hi, exact, dev) -> dict:
     for _ in range(max(1, min(args.warmup, 2))):
         md.rmsd(target, reference, 0)
     torch.cuda.synchronize()
-    times = []
+    times, host_steps = [], []
     for _ in range(args.e2e_steps):
         t0 = time.perf_counter()
         md.rmsd(target, reference, 0)
         times.append(time.perf_counter() - t0)
+        # where the call's host time went (page locking, unlocking, the wait
+        # for the GPU at the end), per step
+        st = D.LAST_HOST_STREAM
+        host_steps.append({"lock_ms": round(st.get("lock_s", 0.0) * 1e3, 1), "unlock_ms": round(st.get("unlock_s", 0.0) * 1e3, 1),
+                     "wait_ms": round(st.get("wait_s", 0.0) * 1e3, 1), "all_locked": st.get("all_locked")})
     t = float(np.mean(times))
     t_med = float(np.median(times))
     # inbound: every frame and the reference frame; outbound: one RMSD per
@@ -572,7 +577,8 @@ def run_e2e(args, F, A, s_lo, s_hi, exact, dev) -> dict:
            "d2h_bytes_per_step": d2h, "ms_per_step": round(t * 1e3, 2),
            "median_ms_per_step": round(t_med * 1e3, 2), "median_value": round(Fe / t_med, 1),
            "frames": Fe, "api": "mdtraj_gb300.rmsd(target, reference, 0) on host float32 arrays",
-           "steps": args.e2e_steps, "step_ms": [round(x * 1e3, 2) for x in times], "host_link": link}
+           "steps": args.e2e_steps, "step_ms": [round(x * 1e3, 2) for x in times], "step_host": host_steps,
+           "host_link": link}
     if link.get("both_gbs"):
         # the step's host traffic over the link's measured two-way rate
         res["host_link_frac"] = round((h2d + d2h) / t / 1e9 / link["both_gbs"], 4)

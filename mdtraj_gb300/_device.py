@@ -3,6 +3,7 @@ libgbrmsd does the work.  Nothing here computes RMSDs."""
 from __future__ import annotations
 
 import os
+import time
 import warnings
 
 import numpy as np
@@ -249,6 +250,9 @@ class HostLocks:
         self.hi = (base + nbytes + page - 1) // page * page
         self.ranges: list[int] = []
         self.ok = nbytes > 0
+        self.locked_bytes = 0
+        self.lock_s = 0.0    # host time spent locking
+        self.unlock_s = 0.0  # host time spent unlocking
 
     def cover(self, end: int) -> None:
         """Locks through the page holding byte end - 1."""
@@ -258,17 +262,30 @@ class HostLocks:
         target = min(self.hi, (end + page - 1) // page * page)
         if target <= self.done:
             return
-        if lib.gbrmsd_host_register(self.done, target - self.done) != 0:
+        t = time.perf_counter()
+        rc = lib.gbrmsd_host_register(self.done, target - self.done)
+        self.lock_s += time.perf_counter() - t
+        if rc != 0:
             self.ok = False
             return
         self.ranges.append(self.done)
+        self.locked_bytes += target - self.done
         self.done = target
 
     def release(self) -> None:
         """Unlocks every range; call once no queued work touches the array."""
+        t = time.perf_counter()
         for p in self.ranges:
             lib.gbrmsd_host_unregister(p)
         self.ranges = []
+        self.unlock_s += time.perf_counter() - t
+
+
+# Where the last rmsd_host_frames call spent its host time (for benchmarks):
+# chunks, bytes page-locked and whether every range could be locked, seconds
+# locking and unlocking, and the host's final wait for the GPU (small when
+# the host loop, not the GPU, set the pace).
+LAST_HOST_STREAM: dict = {}
 
 
 def rmsd_host_frames(x: np.ndarray, ref: "DeviceReference", mode: int, *, g_target: np.ndarray | None = None,
@@ -360,6 +377,9 @@ def rmsd_host_frames(x: np.ndarray, ref: "DeviceReference", mode: int, *, g_targ
         if locks is not None:
             locks.release()
         raise
+    t_wait = time.perf_counter()
+    s_work.synchronize()
+    t_wait = time.perf_counter() - t_wait
     result = np.empty(F, dtype=np.float32)
     copy_rows(result.ctypes.data, 4 * F, out.data_ptr(), 4 * F, 4 * F, 1, 2, s_work.cuda_stream)
     word = np.zeros(n_chunks, dtype=np.int32)
@@ -368,6 +388,12 @@ def rmsd_host_frames(x: np.ndarray, ref: "DeviceReference", mode: int, *, g_targ
     s_in.synchronize()
     if locks is not None:
         locks.release()
+    LAST_HOST_STREAM.clear()
+    LAST_HOST_STREAM.update(chunks=n_chunks, wait_s=t_wait,
+                            locked_bytes=locks.locked_bytes if locks is not None else 0,
+                            all_locked=bool(locks is not None and locks.ok),
+                            lock_s=locks.lock_s if locks is not None else 0.0,
+                            unlock_s=locks.unlock_s if locks is not None else 0.0)
     raise_on_error_word(int(np.bitwise_or.reduce(word)), "rmsd")
     if write_centred and not host_ok:
         cent_h = np.empty((F, 3), dtype=np.float32)
