@@ -203,8 +203,8 @@ __device__ __forceinline__ void issue_chunk(const StreamArgs& p, const void* tma
 // its last frame each warp meets the rest of its CTA at a barrier, and the
 // CTA solves QCP for all of its frames, 32 at a time (one frame per lane,
 // finish_frame_df: no FP64 on the common path), spread over its warps, so
-// that a 10,000-frame call ends one QCP latency (~2-3 us) after its last
-// byte is read instead of a second launch later.  Frames that need the direct
+// that a 10,000-frame call ends one QCP batch (~6 us) after its last byte
+// is read instead of a second launch later.  Frames that need the direct
 // residual are queued in the CTA's slice of the refinement list and refined
 // after a second barrier, one after another, each by the whole CTA.
 //
@@ -279,10 +279,11 @@ __device__ __forceinline__ void refine_one_cta(const RefineArgs& r, const Refine
 }
 
 // Called by every thread of the CTA once its records are written and
-// visible (after a __syncthreads).
+// visible (after a __syncthreads).  nref and part (WARPS partial sums) live
+// in the kernel's dynamic shared memory, after the barriers (fin_smem_bytes).
 template <int LAYOUT, int WARPS>
-__device__ __noinline__ void stream_fin_tail(const FinishArgs& a, const RefineArgs& r, int* nref, int warp,
-                                             int lane) {
+__device__ __noinline__ void stream_fin_tail(const FinishArgs& a, const RefineArgs& r, int* nref, CF* part,
+                                             int warp, int lane) {
   const FinSlice sl = fin_slice(a.n_frames, WARPS);
   const int64_t W = (int64_t)gridDim.x * WARPS;
   const int64_t b0 = (int64_t)blockIdx.x * WARPS;
@@ -299,7 +300,6 @@ __device__ __noinline__ void stream_fin_tail(const FinishArgs& a, const RefineAr
   }
   __syncthreads();
   const int n = *reinterpret_cast<volatile int*>(nref);
-  __shared__ CF part[WARPS];
   for (int e = 0; e < n; ++e) {
     const RefineEntry en = a.refine[sl.base + e];
     if (en.seg >= 0) refine_one_cta<LAYOUT, WARPS>(r, en, part, warp, lane);  // same entry CTA-wide: uniform
@@ -336,8 +336,10 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
   unsigned char* stages = smem + ref_al + (size_t)warp * NSTAGE * STAGE_BYTES;
   uint64_t* bars =
       reinterpret_cast<uint64_t*>(smem + ref_al + (size_t)WARPS * NSTAGE * STAGE_BYTES) + warp * NSTAGE;
-  // FIN: refinement entries the CTA's finish queued
+  // FIN: refinement entries the CTA's finish queued, then the CTA-wide
+  // refinement's per-warp partial sums (16-byte aligned)
   int* fin_nref = reinterpret_cast<int*>(smem + ref_al + (size_t)WARPS * NSTAGE * (STAGE_BYTES + 8));
+  CF* fin_part = reinterpret_cast<CF*>(fin_nref + 4);
 
   if constexpr (REF_SMEM && USE_REF) {
     const float4* src = reinterpret_cast<const float4*>(p.ref);
@@ -555,7 +557,7 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
     // every record of the CTA is written (a warp whose wait ran out leaves
     // some unwritten: the error word already marks the call's results)
     __syncthreads();
-    stream_fin_tail<LAYOUT, WARPS>(fa, ra, fin_nref, warp, lane);
+    stream_fin_tail<LAYOUT, WARPS>(fa, ra, fin_nref, fin_part, warp, lane);
   }
 }
 
@@ -777,9 +779,14 @@ constexpr StreamCfg kCfgs[kNumCfg] = {
 };
 int g_forced_cfg = -1;
 
+// Shared memory of the in-kernel finish: the refinement count (16 bytes)
+// and one float pair per warp (the CTA-wide refinement's partial sums).
+constexpr size_t kFinSmemPerWarp = sizeof(float) * 2;
+size_t fin_smem_bytes(int warps) { return align_up(16 + kFinSmemPerWarp * (size_t)warps, 16); }
+
 size_t stream_smem_bytes(const StreamCfg& c, int32_t Ap, bool use_ref, bool fin = false) {
   const size_t ref = (c.ref_smem && use_ref) ? align_up((size_t)Ap * 12, 128) : 0;
-  const size_t fin_state = fin ? 16 : 0;  // the in-kernel finish's refinement count
+  const size_t fin_state = fin ? fin_smem_bytes(c.warps) : 0;
   return ref + (size_t)c.warps * c.nstage * c.cq * 48 + (size_t)c.warps * c.nstage * 8 + fin_state;
 }
 
