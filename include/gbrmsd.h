@@ -142,16 +142,20 @@ int64_t gbrmsd_noalloc_max_frames(int32_t n_atoms);
  * Trajectory.center_coordinates); 0 uses the coordinates as given.
  * method 0: FP32 CUDA-core tiles; method 1: split-BF16 (hi + lo) tcgen05
  * tensor-core tiles with FP32 accumulation.  Both solve QCP per pair in FP32;
- * near-identical pairs are recomputed exactly (compensated inner products,
- * FP64 QCP, direct residual).  ws: gbrmsd_allpairs_workspace_bytes(...).
+ * near-identical pairs (rmsd below 0.75 * scale / sqrt(n_atoms), scale = the
+ * pair's mean squared distance of an atom from its centroid) are recomputed
+ * exactly (compensated inner products, FP64 QCP, direct residual), any
+ * number of them: pairs beyond the workspace's list of 2^22 are found again
+ * by a scan of the output.  ws: gbrmsd_allpairs_workspace_bytes(...).
  */
 size_t gbrmsd_allpairs_workspace_bytes(int64_t n_frames, int32_t n_atoms);
 int gbrmsd_allpairs(const float* x, int64_t n_frames, int32_t n_atoms, int32_t n_padded, int64_t frame_stride,
                     int32_t layout, int32_t centre, int32_t method, float* out, void* ws, size_t ws_bytes,
                     void* stream);
 
-/* Synchronises `stream`; reports how many pairs the last gbrmsd_allpairs on
- * this workspace refined exactly and whether a device error was recorded. */
+/* Synchronises `stream`; reports how many pairs the last gbrmsd_allpairs (or
+ * gbrmsd_cross_rmsd) on this workspace refined exactly (clamped to
+ * INT32_MAX) and whether a device error was recorded. */
 int gbrmsd_allpairs_status(const void* ws, int32_t* refined_pairs, void* stream);
 
 /* ---- Superposition: rotations, in-place alignment, RMSF --------------------

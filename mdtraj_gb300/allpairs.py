@@ -58,7 +58,6 @@ def allpairs_rmsd(target, precentered: bool = False, method: str = "tensor") -> 
     ws = D.empty_bytes(lib.gbrmsd_allpairs_workspace_bytes(F, A), device)
     out = allpairs_device(x_dev, F, A, n_padded, _lib.ATOM_MAJOR, centre=not precentered, method=method, ws=ws)
     result = D.to_host(out, stream)
-    # raises when the device recorded an error (an expired wait, a full
-    # refinement list)
+    # raises when the device recorded an error (an expired wait)
     check(lib.gbrmsd_allpairs_status(ws.data_ptr(), None, stream))
     return result

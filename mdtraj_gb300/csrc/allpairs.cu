@@ -9,10 +9,11 @@
 //                         buffering): the yardstick for the tensor path.
 //   pair epilogue         FP32 QCP on the quartic normalised by its upper
 //                         bound; msd = 2 lam0 (1 - x) / n.  Pairs closer than
-//                         0.25 * scale / sqrt(n) (scale = (Ga + Gb) / 2n)
-//                         are queued for allpairs_refine_kernel.
-//   allpairs_refine_kernel warp per queued pair: compensated M, FP64 QCP,
-//                         then the direct residual |R a_i - a_j|^2.
+//                         0.75 * scale / sqrt(n) (scale = (Ga + Gb) / 2n)
+//                         are queued for allpairs_refine_kernel (marked NaN
+//                         in the output when the queue is full).
+//   allpairs_refine_kernel warp per queued (or marked) pair: compensated M,
+//                         FP64 QCP, then the direct residual |R a_i - a_j|^2.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <math.h>
@@ -252,8 +253,98 @@ __global__ void __launch_bounds__(256, 1) allpairs_fp32_kernel(const Fp32Args p)
 // Refinement of near-identical pairs (warp per pair)
 // ---------------------------------------------------------------------------
 
-// Cross: i indexes X32/G (database), j indexes X32b/Gb (query set) and the
-// result goes to the request's output row; all-pairs: X32b == X32.
+// One pair (i, j), the whole warp: compensated M, FP64 QCP, then the direct
+// residual |R a_i - a_j|^2 with R rounded to float.  Cross: i indexes X32/G
+// (database), j indexes X32b/Gb (query set) and the result goes to the
+// request's output row; all-pairs: X32b == X32, both triangles written.
+template <bool CROSS>
+__device__ __forceinline__ void refine_pair(int64_t i, int64_t j, int lane, const float* __restrict__ X32,
+                                            const double* __restrict__ G, int64_t F, int32_t A, int32_t kpad,
+                                            float* __restrict__ out, const float* __restrict__ X32b,
+                                            const double* __restrict__ Gb, int64_t Fb,
+                                            const gbrmsd_cross_request_t* reqs, const int32_t* colreq) {
+  const float* ai[3] = {X32 + (size_t)(3 * i) * kpad, X32 + (size_t)(3 * i + 1) * kpad, X32 + (size_t)(3 * i + 2) * kpad};
+  const float* bj[3] = {X32b + (size_t)(3 * j) * kpad, X32b + (size_t)(3 * j + 1) * kpad,
+                        X32b + (size_t)(3 * j + 2) * kpad};
+  // compensated 3x3 inner product
+  CF v[16];
+#pragma unroll
+  for (int t = 0; t < 16; ++t) v[t] = cf_zero();
+  for (int32_t k0 = 0; k0 < A; k0 += 32 * 4) {
+    float part[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int32_t k = k0 + lane + 32 * u;
+      if (k < A) {
+        const float a[3] = {ai[0][k], ai[1][k], ai[2][k]};
+        const float b[3] = {bj[0][k], bj[1][k], bj[2][k]};
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+          for (int d = 0; d < 3; ++d) part[3 * c + d] = fmaf(a[c], b[d], part[3 * c + d]);
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < 9; ++t) cf_add(v[t], part[t]);
+  }
+  warp_xpose_reduce16(v, lane);
+  double m[9];
+#pragma unroll
+  for (int t = 0; t < 9; ++t) {
+    const float hi = __shfl_sync(FULL_MASK, v[0].hi, 2 * t);
+    const float lo = __shfl_sync(FULL_MASK, v[0].lo, 2 * t);
+    m[t] = (double)hi + (double)lo;
+  }
+  const double ga = G[i], gb = Gb[j];
+  int iters = 0;
+  const double lam = qcp_lambda_max(m, ga, gb, &iters);
+  double rot[9];
+  qcp_rotation(m, lam, rot);
+  float R[9];
+#pragma unroll
+  for (int t = 0; t < 9; ++t) R[t] = (float)rot[t];
+  CF acc = cf_zero();
+  for (int32_t k0 = 0; k0 < A; k0 += 32 * 4) {
+    float part = 0.f;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int32_t k = k0 + lane + 32 * u;
+      if (k < A) {
+        const float a0 = ai[0][k], a1 = ai[1][k], a2 = ai[2][k];
+        const float rx = fmaf(R[0], a0, fmaf(R[1], a1, R[2] * a2)) - bj[0][k];
+        const float ry = fmaf(R[3], a0, fmaf(R[4], a1, R[5] * a2)) - bj[1][k];
+        const float rz = fmaf(R[6], a0, fmaf(R[7], a1, R[8] * a2)) - bj[2][k];
+        part = fmaf(rx, rx, fmaf(ry, ry, fmaf(rz, rz, part)));
+      }
+    }
+    cf_add(acc, part);
+  }
+#pragma unroll
+  for (int mm = 16; mm >= 1; mm >>= 1) {
+    CF o;
+    o.hi = __shfl_xor_sync(FULL_MASK, acc.hi, mm);
+    o.lo = __shfl_xor_sync(FULL_MASK, acc.lo, mm);
+    acc = cf_add2(acc, o);
+  }
+  if (lane == 0) {
+    double msd = cf_to_double(acc) / (double)A;
+    if (!(msd > 0.0)) msd = 0.0;
+    const float r = (float)sqrt(msd);
+    if (CROSS) {
+      const CrossCol cv = cross_col(reqs, colreq, j, Fb);
+      if (cv.row != nullptr) cv.row[i - cv.db0] = r;
+    } else {
+      out[i * F + j] = r;
+      out[j * F + i] = r;
+    }
+  }
+}
+
+// Refinement, one warp per pair: first the queued pairs, then, when the
+// list overflowed (count above rcap), every output slot holding the
+// refine_marker() NaN -- all-pairs: the upper triangle row by row; cross:
+// each request's output row by query column.  *refined receives the number
+// of pairs refined by both.
 template <bool CROSS>
 __global__ void __launch_bounds__(256) allpairs_refine_kernel(const float* __restrict__ X32,
                                                               const double* __restrict__ G, int64_t F, int32_t A,
@@ -262,89 +353,49 @@ __global__ void __launch_bounds__(256) allpairs_refine_kernel(const float* __res
                                                               const float* __restrict__ X32b,
                                                               const double* __restrict__ Gb, int64_t Fb,
                                                               const gbrmsd_cross_request_t* reqs,
-                                                              const int32_t* colreq) {
+                                                              const int32_t* colreq, unsigned long long* refined) {
   const int lane = threadIdx.x & 31;
   const int64_t W = (int64_t)gridDim.x * (blockDim.x >> 5);
-  int n = *reinterpret_cast<const volatile int*>(rc);
-  if (n > rcap) n = rcap;
-  for (int64_t e = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); e < n; e += W) {
-    const int64_t i = rl[e].i, j = rl[e].j;
-    const float* ai[3] = {X32 + (size_t)(3 * i) * kpad, X32 + (size_t)(3 * i + 1) * kpad, X32 + (size_t)(3 * i + 2) * kpad};
-    const float* bj[3] = {X32b + (size_t)(3 * j) * kpad, X32b + (size_t)(3 * j + 1) * kpad,
-                          X32b + (size_t)(3 * j + 2) * kpad};
-    // compensated 3x3 inner product
-    CF v[16];
-#pragma unroll
-    for (int t = 0; t < 16; ++t) v[t] = cf_zero();
-    for (int32_t k0 = 0; k0 < A; k0 += 32 * 4) {
-      float part[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int32_t k = k0 + lane + 32 * u;
-        if (k < A) {
-          const float a[3] = {ai[0][k], ai[1][k], ai[2][k]};
-          const float b[3] = {bj[0][k], bj[1][k], bj[2][k]};
-#pragma unroll
-          for (int c = 0; c < 3; ++c)
-#pragma unroll
-            for (int d = 0; d < 3; ++d) part[3 * c + d] = fmaf(a[c], b[d], part[3 * c + d]);
+  const int64_t gw = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int n_all = *reinterpret_cast<const volatile int*>(rc);
+  const int n = n_all < rcap ? n_all : rcap;
+  if (gw == 0 && lane == 0 && n > 0) atomicAdd(refined, (unsigned long long)n);
+  for (int64_t e = gw; e < n; e += W)
+    refine_pair<CROSS>(rl[e].i, rl[e].j, lane, X32, G, F, A, kpad, out, X32b, Gb, Fb, reqs, colreq);
+  if (n_all <= rcap) return;
+  unsigned long long found = 0;
+  if (!CROSS) {
+    for (int64_t i = gw; i < F; i += W) {
+      const float* row = out + i * F;
+      for (int64_t j0 = i + 1; j0 < F; j0 += 32) {
+        const int64_t j = j0 + lane;
+        unsigned hit = __ballot_sync(FULL_MASK, j < F && isnan(row[j]));
+        while (hit) {
+          const int b = __ffs(hit) - 1;
+          hit &= hit - 1;
+          refine_pair<false>(i, j0 + b, lane, X32, G, F, A, kpad, out, X32b, Gb, Fb, reqs, colreq);
+          ++found;
         }
       }
-#pragma unroll
-      for (int t = 0; t < 9; ++t) cf_add(v[t], part[t]);
     }
-    warp_xpose_reduce16(v, lane);
-    double m[9];
-#pragma unroll
-    for (int t = 0; t < 9; ++t) {
-      const float hi = __shfl_sync(FULL_MASK, v[0].hi, 2 * t);
-      const float lo = __shfl_sync(FULL_MASK, v[0].lo, 2 * t);
-      m[t] = (double)hi + (double)lo;
-    }
-    const double ga = G[i], gb = Gb[j];
-    int iters = 0;
-    const double lam = qcp_lambda_max(m, ga, gb, &iters);
-    double rot[9];
-    qcp_rotation(m, lam, rot);
-    float R[9];
-#pragma unroll
-    for (int t = 0; t < 9; ++t) R[t] = (float)rot[t];
-    CF acc = cf_zero();
-    for (int32_t k0 = 0; k0 < A; k0 += 32 * 4) {
-      float part = 0.f;
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int32_t k = k0 + lane + 32 * u;
-        if (k < A) {
-          const float a0 = ai[0][k], a1 = ai[1][k], a2 = ai[2][k];
-          const float rx = fmaf(R[0], a0, fmaf(R[1], a1, R[2] * a2)) - bj[0][k];
-          const float ry = fmaf(R[3], a0, fmaf(R[4], a1, R[5] * a2)) - bj[1][k];
-          const float rz = fmaf(R[6], a0, fmaf(R[7], a1, R[8] * a2)) - bj[2][k];
-          part = fmaf(rx, rx, fmaf(ry, ry, fmaf(rz, rz, part)));
+  } else {
+    for (int64_t j = gw; j < Fb; j += W) {
+      const CrossCol cv = cross_col(reqs, colreq, j, Fb);
+      if (cv.row == nullptr) continue;
+      const int64_t end = cv.db1 < F ? cv.db1 : F;
+      for (int64_t i0 = cv.db0; i0 < end; i0 += 32) {
+        const int64_t i = i0 + lane;
+        unsigned hit = __ballot_sync(FULL_MASK, i < end && isnan(cv.row[i - cv.db0]));
+        while (hit) {
+          const int b = __ffs(hit) - 1;
+          hit &= hit - 1;
+          refine_pair<true>(i0 + b, j, lane, X32, G, F, A, kpad, out, X32b, Gb, Fb, reqs, colreq);
+          ++found;
         }
-      }
-      cf_add(acc, part);
-    }
-#pragma unroll
-    for (int mm = 16; mm >= 1; mm >>= 1) {
-      CF o;
-      o.hi = __shfl_xor_sync(FULL_MASK, acc.hi, mm);
-      o.lo = __shfl_xor_sync(FULL_MASK, acc.lo, mm);
-      acc = cf_add2(acc, o);
-    }
-    if (lane == 0) {
-      double msd = cf_to_double(acc) / (double)A;
-      if (!(msd > 0.0)) msd = 0.0;
-      const float r = (float)sqrt(msd);
-      if (CROSS) {
-        const CrossCol cv = cross_col(reqs, colreq, j, Fb);
-        if (cv.row != nullptr) cv.row[i - cv.db0] = r;
-      } else {
-        out[i * F + j] = r;
-        out[j * F + i] = r;
       }
     }
   }
+  if (lane == 0 && found) atomicAdd(refined, found);
 }
 
 struct ApWs {
@@ -560,12 +611,18 @@ size_t gbrmsd_allpairs_workspace_bytes(int64_t n_frames, int32_t n_atoms) {
 int gbrmsd_allpairs_status(const void* ws, int32_t* refined_pairs, void* stream) {
   clear_error();
   if (!ws) return set_error(GBRMSD_E_INVALID, "allpairs_status: null workspace");
-  int h[2] = {0, 0};
+  // header: [0] error word, [1] list count (saturates near the list's
+  // capacity), [2..3] pairs refined (list and overflow scan)
+  int h[4] = {0, 0, 0, 0};
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   GB_CUDA_TRY(cudaMemcpyAsync(h, ws, sizeof(h), cudaMemcpyDeviceToHost, st), "copy allpairs header");
   GB_CUDA_TRY(cudaStreamSynchronize(st), "sync");
-  if (refined_pairs) *refined_pairs = h[1];
-  if (h[0]) return set_error(GBRMSD_E_DEVICE, "allpairs device error word 0x%x (1 = wait expired, 4 = refinement list full)", h[0]);
+  if (refined_pairs) {
+    unsigned long long total;
+    memcpy(&total, h + 2, sizeof(total));
+    *refined_pairs = (int32_t)std::min<unsigned long long>(total, (unsigned long long)INT32_MAX);
+  }
+  if (h[0]) return set_error(GBRMSD_E_DEVICE, "allpairs device error word 0x%x (1 = wait expired)", h[0]);
   return GBRMSD_OK;
 }
 
@@ -591,13 +648,13 @@ int gbrmsd_allpairs(const float* x, int64_t n_frames, int32_t n_atoms, int32_t n
     return set_error(GBRMSD_E_WORKSPACE, "allpairs: workspace needs %zu bytes", L.total);
   const int32_t kpad = (n_atoms + 63) / 64 * 64;
   unsigned char* w = static_cast<unsigned char*>(ws);
-  int* hdr = reinterpret_cast<int*>(w);  // [0] err, [1] refine count
+  int* hdr = reinterpret_cast<int*>(w);  // [0] err, [1] list count, [2..3] pairs refined
   float* X32 = reinterpret_cast<float*>(w + L.x32);
   __nv_bfloat16* Xhi = reinterpret_cast<__nv_bfloat16*>(w + L.hi);
   __nv_bfloat16* Xlo = reinterpret_cast<__nv_bfloat16*>(w + L.lo);
   double* G = reinterpret_cast<double*>(w + L.g);
   PairRefine* rl = reinterpret_cast<PairRefine*>(w + L.rl);
-  GB_CUDA_TRY(cudaMemsetAsync(hdr, 0, 8, st), "memset allpairs header");
+  GB_CUDA_TRY(cudaMemsetAsync(hdr, 0, 16, st), "memset allpairs header");
   allpairs_prep_kernel<<<sm_count() * 8, 256, 0, st>>>(x, n_frames, n_atoms, n_padded, frame_stride, layout,
                                                        centre ? 1 : 0, kpad, X32, Xhi, Xlo, G);
   GB_CUDA_TRY(cudaGetLastError(), "launch allpairs_prep_kernel");
@@ -635,7 +692,8 @@ int gbrmsd_allpairs(const float* x, int64_t n_frames, int32_t n_atoms, int32_t n
     prof_end(st);
   }
   allpairs_refine_kernel<false><<<sm_count() * 4, 256, 0, st>>>(X32, G, n_frames, n_atoms, kpad, rl, hdr + 1, L.rcap,
-                                                                 out, X32, G, n_frames, nullptr, nullptr);
+                                                                 out, X32, G, n_frames, nullptr, nullptr,
+                                                                 reinterpret_cast<unsigned long long*>(hdr + 2));
   GB_CUDA_TRY(cudaGetLastError(), "launch allpairs_refine_kernel");
   return GBRMSD_OK;
 }
@@ -698,7 +756,7 @@ int gbrmsd_cross_rmsd(const void* db_set, int64_t db_capacity, int64_t n_db, con
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   unsigned char* w = static_cast<unsigned char*>(ws);
   int* hdr = reinterpret_cast<int*>(w);
-  GB_CUDA_TRY(cudaMemsetAsync(hdr, 0, 8, st), "memset cross header");
+  GB_CUDA_TRY(cudaMemsetAsync(hdr, 0, 16, st), "memset cross header");
   if (cc.max_tiles == 0) return GBRMSD_OK;
   auto* dreq = reinterpret_cast<gbrmsd_cross_request_t*>(w + W.reqs);
   auto* dcol = reinterpret_cast<int32_t*>(w + W.colreq);
@@ -770,7 +828,8 @@ int gbrmsd_cross_rmsd(const void* db_set, int64_t db_capacity, int64_t n_db, con
     prof_end(st);
   }
   allpairs_refine_kernel<true><<<sm_count() * 4, 256, 0, st>>>(X32a, Ga, n_db, n_atoms, La.kpad, rl, hdr + 1, W.rcap,
-                                                                nullptr, X32b, Gb, query_capacity, dreq, dcol);
+                                                                nullptr, X32b, Gb, query_capacity, dreq, dcol,
+                                                                reinterpret_cast<unsigned long long*>(hdr + 2));
   GB_CUDA_TRY(cudaGetLastError(), "launch cross refine kernel");
   return GBRMSD_OK;
 }

@@ -29,7 +29,10 @@ struct AllPairsDims {
   int64_t rows;    // 3 * n_frames
 };
 
-constexpr int DEV_ERR_REFINE_OVERFLOW = 4;
+// Result slot of a pair that needs refinement but found the refinement list
+// full: a quiet NaN, which the refinement kernel finds by scanning the output
+// (a non-finite input gives NaN as well; refining it again gives NaN again).
+__device__ __forceinline__ float refine_marker() { return __int_as_float(0x7fc00000); }
 
 // Explicitly rounded FP32 operations for the pair epilogue.  The epilogue is
 // inlined at several points of the tile kernels (inside the fold loop, after
@@ -254,18 +257,23 @@ __device__ __forceinline__ float qcp_msd_f32(const float (&m)[9], float ga, floa
   return msd;
 }
 
-// Refinement threshold of a pair: r < 0.25 * scale * sqrt(1/n), scale =
+// Refinement threshold of a pair: r < 0.75 * scale * sqrt(1/n), scale =
 // (Ga + Gb) / 2n (explicitly rounded for the same reason as the QCP above).
+// The msd error of the split-BF16 M grows like scale / sqrt(n): summing the
+// three BF16 products exactly it stays below 3.4e-5 * scale / sqrt(n) (all
+// 44,850 pairs each of 300 noisy rotated copies of 257 and of 1,000 atoms,
+// 0.001-0.4 nm noise), and the tensor core's FP32 accumulation doubles it.
+// The rmsd error is the msd error over 2 r, so above the threshold it stays
+// below ~4.5e-5 nm (measured 1.2-1.4e-4 nm at the former 0.25).
 __device__ __forceinline__ bool pair_needs_refine(float r, float ga, float gb, float inv_n) {
   const float scale = rn_mul(rn_mul(0.5f, rn_add(ga, gb)), inv_n);
-  return r < rn_mul(rn_mul(0.25f, scale), sqrtf(inv_n));
+  return r < rn_mul(rn_mul(0.75f, scale), sqrtf(inv_n));
 }
 
 // Writes the pair's rmsd to both triangles (i < j) or 0 on the diagonal and
-// queues pairs the FP32 QCP cannot resolve for exact refinement.  The error
-// of M (split-BF16 or FP32 accumulation) is ~1e-6 * scale / sqrt(n) in msd
-// units, i.e. <= 2e-5 nm in rmsd above r = 0.25 * scale / sqrt(n) (scale =
-// (Ga + Gb) / 2n in nm^2); below it the pair is recomputed.
+// queues pairs the FP32 QCP cannot resolve, or that lie below the refinement
+// threshold, for exact refinement.  When the list is full the pair's two
+// slots get refine_marker() instead, and the refinement kernel scans for it.
 // (ga, gb: the two frames' traces rounded to float.)
 __device__ __forceinline__ void pair_epilogue_g(int64_t i, int64_t j, const float (&m)[9], float ga, float gb,
                                                 float inv_n, int64_t F, float* __restrict__ out, PairRefine* rl,
@@ -276,16 +284,18 @@ __device__ __forceinline__ void pair_epilogue_g(int64_t i, int64_t j, const floa
   }
   bool unresolved;
   const float msd = qcp_msd_f32(m, ga, gb, inv_n, unresolved);
-  const float r = sqrtf(msd);
-  out[i * F + j] = r;
-  out[j * F + i] = r;
+  float r = sqrtf(msd);
   if (unresolved || pair_needs_refine(r, ga, gb, inv_n)) {
-    const int slot = atomicAdd(rc, 1);
+    // the count is read first so that it stops growing once the list is
+    // full (it exceeds rcap by at most the pairs in flight)
+    const int slot = *reinterpret_cast<volatile int*>(rc) < rcap ? atomicAdd(rc, 1) : rcap;
     if (slot < rcap)
       rl[slot] = PairRefine{(int32_t)i, (int32_t)j};
     else
-      atomicOr(err, DEV_ERR_REFINE_OVERFLOW);
+      r = refine_marker();
   }
+  out[i * F + j] = r;
+  out[j * F + i] = r;
 }
 
 __device__ __forceinline__ void pair_epilogue(int64_t i, int64_t j, const float (&m)[9], const double* __restrict__ G,
@@ -326,15 +336,17 @@ __device__ __forceinline__ void cross_pair(int64_t i, int64_t j, const float (&m
                                            float inv_n, float* dst, PairRefine* rl, int* rc, int rcap, int* err) {
   bool unresolved;
   const float msd = qcp_msd_f32(m, ga, gb, inv_n, unresolved);
-  const float r = sqrtf(msd);
-  *dst = r;
+  float r = sqrtf(msd);
   if (unresolved || pair_needs_refine(r, ga, gb, inv_n)) {
-    const int slot = atomicAdd(rc, 1);
+    // the count is read first so that it stops growing once the list is
+    // full (it exceeds rcap by at most the pairs in flight)
+    const int slot = *reinterpret_cast<volatile int*>(rc) < rcap ? atomicAdd(rc, 1) : rcap;
     if (slot < rcap)
       rl[slot] = PairRefine{(int32_t)i, (int32_t)j};
     else
-      atomicOr(err, DEV_ERR_REFINE_OVERFLOW);
+      r = refine_marker();
   }
+  *dst = r;
 }
 
 }  // namespace gb

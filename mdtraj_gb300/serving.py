@@ -214,7 +214,7 @@ class _Slot:
         self.ws_buf = None
         # the batch's error word and refined-pair count, copied to the host
         # right after its kernels (read once its event has fired)
-        self.hdr = torch.zeros(2, dtype=torch.int32, pin_memory=True)
+        self.hdr = torch.zeros(4, dtype=torch.int32, pin_memory=True)  # error word, list count, refined (int64)
 
 
 class RmsdServer:
@@ -335,7 +335,7 @@ class RmsdServer:
             table = request_table([(r._out.data_ptr(), r._p0, r.n_query, r.db0, r.db1) for r in batch])
             ws = slot.ws.get(self.n_db, self.qcap, len(batch))
             cross_launch(self.db, self.n_db, self.qset, table, len(batch), self.method, ws, s.cuda_stream)
-            slot.hdr.copy_(ws[:8].view(torch.int32), non_blocking=True)
+            slot.hdr.copy_(ws[:16].view(torch.int32), non_blocking=True)
             t_ev[1].record(s)
             if self.result_to_host:
                 for r in batch:
@@ -372,7 +372,8 @@ class RmsdServer:
         return r
 
     def _complete(self, slot: _Slot, now: float, keep_results: bool) -> list:
-        err, refined = (int(v) for v in slot.hdr.tolist())  # copied before the batch's event
+        err = int(slot.hdr[0])  # copied before the batch's event
+        refined = int(slot.hdr[2:].view(torch.int64)[0])
         if err:
             raise _lib.GbrmsdError(_lib.E_DEVICE, "cross RMSD batch: device error word 0x%x (1 = wait expired, "
                                                   "4 = refinement list full)" % err)

@@ -133,3 +133,69 @@ def test_frame_range_covers_frames_once():
             assert np.all(seen == 1)
     with pytest.raises(ValueError):
         frame_range(10, 2, 2)
+
+
+def _fp64_rows(xyz, requests, precentered, method):
+    """FP64 Kabsch RMSD of each range's frame pairs (the oracle), as the
+    per-rank scorer of allpairs_sharded."""
+    from oracle import fp64
+
+    out = []
+    for i0, i1, j0, j1 in requests:
+        blk = np.empty((i1 - i0, j1 - j0), np.float32)
+        for b, j in enumerate(range(j0, j1)):
+            blk[:, b] = fp64.kabsch_rmsd(xyz[i0:i1], xyz[j])
+        out.append(blk)
+    return out
+
+
+def _allpairs_worker(rank, world, port, q):
+    import torch.distributed as dist
+
+    from mdtraj_gb300 import synth
+    from mdtraj_gb300.shard import allpairs_sharded
+
+    os.environ.update({"MASTER_ADDR": "127.0.0.1", "MASTER_PORT": str(port)})
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        _, x = synth.single_reference_frames(61, 17, seed=21, sigma=0.2)
+        q.put((rank, allpairs_sharded(x, score=_fp64_rows)))
+    finally:
+        dist.destroy_process_group()
+
+
+@pytest.mark.parametrize("world", [2, 3])
+def test_allpairs_sharded_over_gloo_ranks_equals_the_whole_triangle(world):
+    """Each rank computes its run of the upper triangle's blocks; after one
+    all-gather every rank holds the same symmetric matrix, equal bit for bit
+    to the whole triangle computed at once, diagonal 0."""
+    import torch.multiprocessing as mp
+
+    from mdtraj_gb300 import synth
+    from mdtraj_gb300.shard import default_block, row_requests
+
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_allpairs_worker, args=(r, world, port, q)) for r in range(world)]
+    for p in procs:
+        p.start()
+    res = sorted((q.get(timeout=180) for _ in range(world)), key=lambda v: v[0])
+    for p in procs:
+        p.join(60)
+    assert all(p.exitcode == 0 for p in procs), [p.exitcode for p in procs]
+    _, x = synth.single_reference_frames(61, 17, seed=21, sigma=0.2)
+    (whole,) = _fp64_rows(x, [(0, 61, 0, 61)], False, "tensor")
+    want = np.triu(whole, 1) + np.triu(whole, 1).T
+    for _, out in res:
+        np.testing.assert_array_equal(out, want)
+    # the ranks' ranges cover the upper triangle once, a frame row at most once per rank
+    B = default_block(61, world)
+    cover = np.zeros((61, 61), int)
+    for r in range(world):
+        reqs = row_requests(61, B, r, world)
+        assert len({i0 for i0, _, _, _ in reqs}) == len(reqs)
+        for i0, i1, j0, j1 in reqs:
+            cover[i0:i1, j0:j1] += 1
+    iu = np.triu_indices(61, 1)
+    assert cover.max() == 1 and np.all(cover[iu] == 1)
