@@ -468,20 +468,12 @@ __host__ __device__ __forceinline__ bool qcp_rotation(const double* m, double la
   return true;
 }
 
-// Rotation for the refinement pass (near-identical frames), in FP32 past the
-// subtraction of lam: the refined residual sum |R (a - mu) - b|^2 is at its
-// minimum over rotations, so an error e in R changes it by O(e^2), and a
-// float adjugate (e ~ 1e-7 where the top eigenvalue is simple) suffices.
-// Where it is (nearly) double, the adjugate is rounding noise in FP32 and
-// the FP64 qcp_rotation (with its shift) is used instead.  ~25 FP64
-// operations against ~200 (the FP64 rotation's sqrt and division alone are
-// software sequences of FP64 operations).
-__host__ __device__ __forceinline__ void qcp_rotation_refine(const double* m, double lam, float* rot) {
-  const float b00 = (float)((m[0] + m[4] + m[8]) - lam), b11 = (float)((m[0] - m[4] - m[8]) - lam);
-  const float b22 = (float)((m[4] - m[0] - m[8]) - lam), b33 = (float)((m[8] - m[0] - m[4]) - lam);
-  float mf[9];
-#pragma unroll
-  for (int i = 0; i < 9; ++i) mf[i] = (float)m[i];
+// FP32 core of the refinement rotation: B = K - lam I with its diagonal
+// (b00..b33, already rounded past the subtraction of lam) and M in float.
+// Returns false, leaving rot untouched, where the adjugate is FP32 rounding
+// noise (top eigenvalue (nearly) double) and the FP64 rotation is needed.
+__host__ __device__ __forceinline__ bool qcp_rotation_refine_f32(float b00, float b11, float b22, float b33,
+                                                                 const float (&mf)[9], float* rot) {
   const float b01 = mf[5] - mf[7], b02 = mf[6] - mf[2], b03 = mf[1] - mf[3];
   const float b12 = mf[1] + mf[3], b13 = mf[6] + mf[2], b23 = mf[5] + mf[7];
   const float u0 = b00 * b11 - b01 * b01, u1 = b00 * b12 - b01 * b02, u2 = b00 * b13 - b01 * b03;
@@ -524,13 +516,7 @@ __host__ __device__ __forceinline__ void qcp_rotation_refine(const double* m, do
   // double
   const float sk = fabsf(b00) + fabsf(b11) + fabsf(b22) + fabsf(b33);
   const float n = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
-  if (!(best > 1e-4f * sk * sk * sk) || !(n > 1e-30f) || !(n < 1e30f)) {
-    double r64[9];
-    qcp_rotation(m, lam, r64);
-#pragma unroll
-    for (int i = 0; i < 9; ++i) rot[i] = (float)r64[i];
-    return;
-  }
+  if (!(best > 1e-4f * sk * sk * sk) || !(n > 1e-30f) || !(n < 1e30f)) return false;
   const float inv = 1.0f / sqrtf(n);
   const float qw = q[0] * inv, qx = q[1] * inv, qy = q[2] * inv, qz = q[3] * inv;
   const float ww = qw * qw, xx = qx * qx, yy = qy * qy, zz = qz * qz;
@@ -544,6 +530,51 @@ __host__ __device__ __forceinline__ void qcp_rotation_refine(const double* m, do
   rot[6] = 2.0f * (zx - wy);
   rot[7] = 2.0f * (yz + wx);
   rot[8] = ww - xx - yy + zz;
+  return true;
+}
+
+// Rotation for the refinement pass (near-identical frames), in FP32 past the
+// subtraction of lam: the refined residual sum |R (a - mu) - b|^2 is at its
+// minimum over rotations, so an error e in R changes it by O(e^2), and a
+// float adjugate (e ~ 1e-7 where the top eigenvalue is simple) suffices.
+// Where it is (nearly) double, the adjugate is rounding noise in FP32 and
+// the FP64 qcp_rotation (with its shift) is used instead.  ~25 FP64
+// operations against ~200 (the FP64 rotation's sqrt and division alone are
+// software sequences of FP64 operations).
+__host__ __device__ __forceinline__ void qcp_rotation_refine(const double* m, double lam, float* rot) {
+  const float b00 = (float)((m[0] + m[4] + m[8]) - lam), b11 = (float)((m[0] - m[4] - m[8]) - lam);
+  const float b22 = (float)((m[4] - m[0] - m[8]) - lam), b33 = (float)((m[8] - m[0] - m[4]) - lam);
+  float mf[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) mf[i] = (float)m[i];
+  if (qcp_rotation_refine_f32(b00, b11, b22, b33, mf, rot)) return;
+  double r64[9];
+  qcp_rotation(m, lam, r64);
+#pragma unroll
+  for (int i = 0; i < 9; ++i) rot[i] = (float)r64[i];
+}
+
+// The same from float-pair M and lam (the in-kernel finish): the diagonal of
+// B in float pairs, no FP64 instruction unless the FP64 fallback is needed
+// (GB300 issues an FP64 instruction per ~64 cycles of a sub-partition, and
+// the ~25 of qcp_rotation_refine held a refined frame's lane ~2 us).
+__host__ __device__ __forceinline__ void qcp_rotation_refine_dfm(const DF (&m)[9], DF lam, float* rot) {
+  const DF k00 = df_add(df_add(m[0], m[4]), m[8]), k11 = df_sub(df_sub(m[0], m[4]), m[8]);
+  const DF k22 = df_sub(df_sub(m[4], m[0]), m[8]), k33 = df_sub(df_sub(m[8], m[0]), m[4]);
+  const DF d0 = df_sub(k00, lam), d1 = df_sub(k11, lam), d2 = df_sub(k22, lam), d3 = df_sub(k33, lam);
+  float mf[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) mf[i] = GB_FADD(m[i].hi, m[i].lo);
+  if (qcp_rotation_refine_f32(GB_FADD(d0.hi, d0.lo), GB_FADD(d1.hi, d1.lo), GB_FADD(d2.hi, d2.lo),
+                              GB_FADD(d3.hi, d3.lo), mf, rot))
+    return;
+  double md[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) md[i] = df_to_double(m[i]);
+  double r64[9];
+  qcp_rotation(md, df_to_double(lam), r64);
+#pragma unroll
+  for (int i = 0; i < 9; ++i) rot[i] = (float)r64[i];
 }
 
 }  // namespace gb

@@ -168,12 +168,24 @@ __device__ __forceinline__ void cursor_unit(Cursor& cur, int64_t u, int32_t S, i
   cur.q1 = (int32_t)(((int64_t)(s + 1) * Q) / S);
 }
 
-// Advances to the next chunk; returns true when a new unit starts.
+// The unit a warp takes at round position v (v = g + k W for warp g): v
+// itself in the full rounds; in the partial last round the highest warps
+// take its units (frames near the start, often the ones closest to the
+// reference and refined, then sit in CTAs that stream one round less), and
+// the others are done (n_units).
+__device__ __forceinline__ int64_t place_unit(int64_t v, const StreamArgs& p) {
+  if (v < p.full_units) return v;
+  const int64_t g = v - p.full_units;  // < W
+  return g >= p.part_shift ? v - p.part_shift : p.n_frames * p.splits;
+}
+
+// Advances to the next chunk; returns true when a new unit starts (a unit of
+// the partial round is a warp's last).
 template <int CQ>
-__device__ __forceinline__ bool cursor_next(Cursor& cur, int64_t W, int32_t S, int32_t Q) {
+__device__ __forceinline__ bool cursor_next(Cursor& cur, int64_t W, int32_t S, int32_t Q, const StreamArgs& p) {
   cur.c += 1;
   if (cur.q0 + cur.c * CQ >= cur.q1) {
-    cursor_unit<CQ>(cur, cur.unit + W, S, Q);
+    cursor_unit<CQ>(cur, cur.unit >= p.full_units ? p.n_frames * p.splits : place_unit(cur.unit + W, p), S, Q);
     return true;
   }
   return false;
@@ -210,19 +222,43 @@ __device__ __forceinline__ void issue_chunk(const StreamArgs& p, const void* tma
 //
 // CTA-local frame i of CTA b belongs to warp w = i % WARPS, round
 // r = i / WARPS: unit b * WARPS + w + r * W (W warps in the grid).
+// Bytes of the in-kernel finish's state in shared memory (refinement count,
+// 16 bytes, then one float pair per warp), 16-byte aligned; the host's
+// fin_smem_bytes gives the same figure.
+template <int WARPS>
+constexpr size_t kFinStateBytes = (16 + 8 * (size_t)WARPS + 15) / 16 * 16;
+
+// The CTA's frames with one unit per frame, dealt as place_unit deals them:
+// warp w's k-th frame is b0 + w + k W for k < full, and in the partial round
+// (warps w >= w0 only) full W + b0 + w - shift.  Local index i (the order of
+// the CTA's records and of its finish): w + k WARPS for k < full, then
+// full WARPS + w - w0.
 struct FinSlice {
-  int64_t n;     // frames of this CTA
-  int64_t base;  // first refinement-list entry of this CTA (frames of lower CTAs)
+  int64_t n;      // frames of this CTA
+  int64_t base;   // first refinement-list entry of this CTA (frames of lower CTAs)
+  int64_t full;   // full rounds
+  int64_t shift;  // W - (frames of the partial round)
+  int64_t w0;     // first warp of this CTA with a frame in the partial round
 };
 
 __device__ __forceinline__ FinSlice fin_slice(int64_t F, int warps) {
   const int64_t W = (int64_t)gridDim.x * warps;
   const int64_t b0 = (int64_t)blockIdx.x * warps;
-  const int64_t full = F / W, rem = F - full * W;
   FinSlice s;
-  s.n = full * warps + min((int64_t)warps, max((int64_t)0, rem - b0));
-  s.base = full * warps * (int64_t)blockIdx.x + min(rem, b0);
+  s.full = F / W;
+  s.shift = W - (F - s.full * W);
+  s.w0 = min((int64_t)warps, max((int64_t)0, s.shift - b0));
+  s.n = s.full * warps + (warps - s.w0);
+  s.base = s.full * warps * (int64_t)blockIdx.x + max((int64_t)0, b0 - s.shift);
   return s;
+}
+
+// Frame of local index i (see FinSlice).
+__device__ __forceinline__ int64_t fin_frame(const FinSlice& s, int64_t i, int warps) {
+  const int64_t W = (int64_t)gridDim.x * warps;
+  const int64_t b0 = (int64_t)blockIdx.x * warps;
+  if (i < s.full * warps) return b0 + (i % warps) + (i / warps) * W;
+  return s.full * W + b0 + (i - s.full * warps + s.w0) - s.shift;
 }
 
 // Direct residual of one queued frame by the whole CTA (WARPS warps): every
@@ -280,21 +316,30 @@ __device__ __forceinline__ void refine_one_cta(const RefineArgs& r, const Refine
 
 // Called by every thread of the CTA once its records are written and
 // visible (after a __syncthreads).  nref and part (WARPS partial sums) live
-// in the kernel's dynamic shared memory, after the barriers (fin_smem_bytes).
+// in the kernel's dynamic shared memory, after the barriers (fin_smem_bytes);
+// with a.rec_smem the records follow them (srec, FREC_FLOATS per frame, in
+// the CTA's local frame order).
 template <int LAYOUT, int WARPS>
 __device__ __noinline__ void stream_fin_tail(const FinishArgs& a, const RefineArgs& r, int* nref, CF* part,
-                                             int warp, int lane) {
+                                             const float* srec, int warp, int lane) {
   const FinSlice sl = fin_slice(a.n_frames, WARPS);
-  const int64_t W = (int64_t)gridDim.x * WARPS;
-  const int64_t b0 = (int64_t)blockIdx.x * WARPS;
   const DF inv = DF{a.inv_hi, a.inv_lo};
+  RefDF rv;
+  rv.g = DF{0.f, 0.f};
+  for (int k = 0; k < 3; ++k) rv.sum[k] = DF{0.f, 0.f};
+  if (a.mode != MODE_PRECENTERED) {
+    const RefInfo* ri = a.ref_info;
+    rv.g = DF{ri->g_hi, ri->g_lo};
+    for (int k = 0; k < 3; ++k) rv.sum[k] = DF{ri->sum_hi[k], ri->sum_lo[k]};
+  }
   for (int64_t k = warp; k * 32 < sl.n; k += WARPS) {
     const int64_t i = k * 32 + lane;
     RefineEntry held;
     bool pending = false;
     if (i < sl.n) {
-      const int64_t f = b0 + (i % WARPS) + (i / WARPS) * W;
-      finish_frame_df(reinterpret_cast<const float*>(a.sums + f * SUMS_STRIDE), f, a, inv, &held, &pending);
+      const int64_t f = fin_frame(sl, i, WARPS);
+      const float* rec = a.rec_smem ? srec + i * FREC_FLOATS : reinterpret_cast<const float*>(a.sums + f * SUMS_STRIDE);
+      finish_frame_df(rec, f, a, inv, rv, &held, &pending);
     }
     if (pending) a.refine[sl.base + atomicAdd_block(nref, 1)] = held;
   }
@@ -340,6 +385,8 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
   // refinement's per-warp partial sums (16-byte aligned)
   int* fin_nref = reinterpret_cast<int*>(smem + ref_al + (size_t)WARPS * NSTAGE * (STAGE_BYTES + 8));
   CF* fin_part = reinterpret_cast<CF*>(fin_nref + 4);
+  float* fin_rec = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(fin_nref) + kFinStateBytes<WARPS>);
+  int32_t fin_done = 0;  // frames this warp has recorded
 
   if constexpr (REF_SMEM && USE_REF) {
     const float4* src = reinterpret_cast<const float4*>(p.ref);
@@ -364,14 +411,14 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
   // chunks ahead).
   const void* tm = &tmap;
   Cursor pc, cc;
-  cursor_unit<CQ>(pc, gw, S, Q);
-  cursor_unit<CQ>(cc, gw, S, Q);
+  cursor_unit<CQ>(pc, place_unit(gw, p), S, Q);
+  cursor_unit<CQ>(cc, place_unit(gw, p), S, Q);
   int64_t issued = 0, consumed = 0;
 #pragma unroll 1
   for (int s = 0; s < NSTAGE; ++s) {
     if (pc.unit < n_units) {
       if (lane == 0) issue_chunk<LAYOUT, CQ>(p, tm, pc, stages + s * STAGE_BYTES, &bars[s]);
-      cursor_next<CQ>(pc, W, S, Q);
+      cursor_next<CQ>(pc, W, S, Q, p);
       ++issued;
     }
   }
@@ -469,13 +516,13 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
         fence_proxy_async_smem();
         issue_chunk<LAYOUT, CQ>(p, tm, pc, stages + slot * STAGE_BYTES, &bars[slot]);
       }
-      cursor_next<CQ>(pc, W, S, Q);
+      cursor_next<CQ>(pc, W, S, Q, p);
       ++issued;
     }
     slot = (slot + 1 == NSTAGE) ? 0 : slot + 1;
 
     const int64_t unit = cc.unit;
-    const bool unit_end = cursor_next<CQ>(cc, W, S, Q);
+    const bool unit_end = cursor_next<CQ>(cc, W, S, Q, p);
     if constexpr (MODE != MODE_TRACE) {
       if (pending >= 4 || unit_end) {
 #pragma unroll
@@ -485,6 +532,18 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
     }
     if (unit_end) {
       double* rec = p.sums + unit * SUMS_STRIDE;
+      float* recf = reinterpret_cast<float*>(rec);
+      if constexpr (FIN) {
+        if (fa.rec_smem) {
+          // local index of the frame (FinSlice): w + k WARPS in the full
+          // rounds, full WARPS + w - w0 in the partial one
+          const int64_t w0 = min((int64_t)WARPS, max((int64_t)0, p.part_shift - (int64_t)blockIdx.x * WARPS));
+          const int64_t li = fin_done < p.full_rounds ? warp + (int64_t)fin_done * WARPS
+                                                      : p.full_rounds * WARPS + warp - w0;
+          recf = fin_rec + li * FREC_FLOATS;
+        }
+        ++fin_done;
+      }
       if constexpr (NV == 1) {
         CF v = acc2[0];
 #pragma unroll
@@ -518,7 +577,6 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
           if constexpr (FIN) {
             // float pair (finish_frame_df's record), normalised
             const DF d = df_two_sum(v[0].hi, v[0].lo);
-            float* recf = reinterpret_cast<float*>(rec);
             recf[2 * idx] = d.hi;
             recf[2 * idx + 1] = d.lo;
           } else {
@@ -528,7 +586,6 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
       }
       if (lane == 0 && MODE == MODE_CENTER) {
         if constexpr (FIN) {
-          float* recf = reinterpret_cast<float*>(rec);
           recf[DFREC_SHIFT] = shift[0];
           recf[DFREC_SHIFT + 1] = shift[1];
           recf[DFREC_SHIFT + 2] = shift[2];
@@ -557,7 +614,7 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
     // every record of the CTA is written (a warp whose wait ran out leaves
     // some unwritten: the error word already marks the call's results)
     __syncthreads();
-    stream_fin_tail<LAYOUT, WARPS>(fa, ra, fin_nref, fin_part, warp, lane);
+    stream_fin_tail<LAYOUT, WARPS>(fa, ra, fin_nref, fin_part, fin_rec, warp, lane);
   }
 }
 
@@ -784,10 +841,25 @@ int g_forced_cfg = -1;
 constexpr size_t kFinSmemPerWarp = sizeof(float) * 2;
 size_t fin_smem_bytes(int warps) { return align_up(16 + kFinSmemPerWarp * (size_t)warps, 16); }
 
-size_t stream_smem_bytes(const StreamCfg& c, int32_t Ap, bool use_ref, bool fin = false) {
+// Record slots of the in-kernel finish for the CTA with the most frames
+// (fin_slice: CTA 0), when they are kept in shared memory.
+size_t fin_rec_bytes(int64_t F, int warps, int grid) {
+  const int64_t W = (int64_t)grid * warps;
+  const int64_t n = (F / W) * warps + std::min<int64_t>(warps, F % W);
+  return (size_t)n * FREC_FLOATS * sizeof(float);
+}
+
+size_t stream_smem_bytes(const StreamCfg& c, int32_t Ap, bool use_ref, bool fin = false, size_t rec_bytes = 0) {
   const size_t ref = (c.ref_smem && use_ref) ? align_up((size_t)Ap * 12, 128) : 0;
-  const size_t fin_state = fin ? fin_smem_bytes(c.warps) : 0;
+  const size_t fin_state = fin ? fin_smem_bytes(c.warps) + rec_bytes : 0;
   return ref + (size_t)c.warps * c.nstage * c.cq * 48 + (size_t)c.warps * c.nstage * 8 + fin_state;
+}
+
+// The in-kernel finish keeps its records in shared memory when the largest
+// CTA's slots fit beside the reference and the copy stages (no L2 round
+// trip per frame in the finish); otherwise in the workspace.
+bool fin_rec_smem(const StreamCfg& c, int32_t Ap, int64_t F) {
+  return stream_smem_bytes(c, Ap, true, true, fin_rec_bytes(F, c.warps, sm_count())) <= (size_t)max_dyn_smem();
 }
 
 // The in-kernel finish is built for the 16-warp configurations of the
@@ -935,9 +1007,16 @@ int launch_stream(int layout, int mode, const StreamArgs& args, const StreamCfg&
   StreamArgs a = args;
   a.wait_ns = wait_limit_ns();
   a.skip_unit = skip_unit_hook();
-  const bool use_ref = mode != MODE_TRACE;
-  const size_t smem = stream_smem_bytes(c, a.n_padded, use_ref, fin != nullptr);
   const int grid = sm_count();
+  {
+    const int64_t W = (int64_t)grid * c.warps, units = a.n_frames * a.splits;
+    a.full_rounds = units / W;
+    a.full_units = a.full_rounds * W;
+    a.part_shift = W - (units - a.full_units);
+  }
+  const bool use_ref = mode != MODE_TRACE;
+  const size_t rec_bytes = (fin && fin->rec_smem) ? fin_rec_bytes(a.n_frames, c.warps, sm_count()) : 0;
+  const size_t smem = stream_smem_bytes(c, a.n_padded, use_ref, fin != nullptr, rec_bytes);
   alignas(64) CUtensorMap tm;
   memset(&tm, 0, sizeof(tm));
   if (layout == AXIS_MAJOR) {
@@ -1158,7 +1237,7 @@ int gbrmsd_rmsd_to_reference(const float* x, int64_t n_frames, int32_t n_atoms, 
   sa.sums = reinterpret_cast<double*>(w + L.sums_off);
   sa.err = &hdr->err;
 
-  FinishArgs fa;
+  FinishArgs fa{};
   fa.n_frames = n_frames;
   fa.n_atoms = n_atoms;
   fa.inv_atoms = 1.0 / (double)n_atoms;
@@ -1195,6 +1274,7 @@ int gbrmsd_rmsd_to_reference(const float* x, int64_t n_frames, int32_t n_atoms, 
   fa.inv_hi = (float)fa.inv_atoms;
   fa.inv_lo = (float)(fa.inv_atoms - (double)fa.inv_hi);
   const bool fin = fin_usable(cfg, mode, S, n_padded);
+  fa.rec_smem = fin && fin_rec_smem(cfg, n_padded, n_frames) ? 1 : 0;
   prof_begin(st);
   rc = fin ? launch_stream(layout, mode, sa, cfg, st, &fa, &ra) : launch_stream(layout, mode, sa, cfg, st);
   if (rc) return rc;

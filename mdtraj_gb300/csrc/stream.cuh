@@ -54,6 +54,14 @@ struct StreamArgs {
   uint64_t wait_ns;      // limit of each bounded wait (gbrmsd_set_wait_limit_ns)
   int64_t skip_unit;     // failure-detection test hook: the first chunk of this
                          // unit is never issued (-1: off)
+  // Units are dealt to the W = grid x warps warps in rounds (warp g takes
+  // g, g + W, ...); the partial last round goes to the highest warps: warp
+  // g >= part_shift takes unit full_units + g - part_shift.  Set by the
+  // launcher: full_rounds = units / W, full_units = full_rounds * W,
+  // part_shift = W - (units - full_units).
+  int64_t full_units;
+  int64_t part_shift;
+  int64_t full_rounds;
 };
 
 // Process-wide settings of the failure-detection hooks (stream.cu).
@@ -81,6 +89,7 @@ struct FinishArgs {
   float* out_rot;             // optional, n_frames x 9 (superposition)
   double* out_mu;             // optional with out_rot, n_frames x 3
   float inv_hi, inv_lo;       // 1 / n_atoms as a float pair (in-kernel finish)
+  int32_t rec_smem;           // in-kernel finish: records in shared memory (1) or in sums (0)
 };
 
 }  // namespace gb

@@ -397,6 +397,16 @@ __device__ __forceinline__ void finish_frame(const FrameCtx& c, float* out_rmsd,
 // (j < 13: M, then MODE_CENTER's coordinate sum and trace about the shift),
 // MODE_CENTER's float shift at [DFREC_SHIFT, +3).
 constexpr int DFREC_SHIFT = 26;
+// Floats per record slot of the in-kernel finish when the records are kept
+// in shared memory (13 float pairs and the float shift, padded).
+constexpr int FREC_FLOATS = 32;
+
+// The reference's trace and coordinate sums as float pairs, read once per
+// thread before its frames (MODE_CENTER).
+struct RefDF {
+  DF g;
+  DF sum[3];
+};
 
 // finish_frame for such a record, with no FP64 instruction on the common
 // path (GB300 issues one FP64 instruction per ~64 cycles of a sub-partition;
@@ -406,13 +416,14 @@ constexpr int DFREC_SHIFT = 26;
 //   mu = s + sdA,  Ga = g - sdA . sd,  M = m - sdA (sum_k b_k)^T,
 // runs in float pairs and feeds qcp_lambda_max_dfm directly.  FP64 remains
 // for the double-root polish and for building a refinement entry (rare).
+// rec: the frame's record, in shared memory or in the workspace (written by
+// warps of the same CTA before a __syncthreads, so plain loads see it).
 __device__ __forceinline__ void finish_frame_df(const float* rec, int64_t f, const FinishArgs& a, DF inv,
-                                                RefineEntry* held, bool* pending) {
+                                                const RefDF& rv, RefineEntry* held, bool* pending) {
   const int32_t A = a.n_atoms;
-  const RefInfo* ri = a.ref_info;
   DF m[9];
 #pragma unroll
-  for (int i = 0; i < 9; ++i) m[i] = DF{__ldcg(rec + 2 * i), __ldcg(rec + 2 * i + 1)};
+  for (int i = 0; i < 9; ++i) m[i] = DF{rec[2 * i], rec[2 * i + 1]};
   DF ga, gb, mu[3] = {DF{0.f, 0.f}, DF{0.f, 0.f}, DF{0.f, 0.f}};
   if (a.mode == MODE_PRECENTERED) {
     ga = DF{a.g_target[f], 0.f};
@@ -421,19 +432,18 @@ __device__ __forceinline__ void finish_frame_df(const float* rec, int64_t f, con
     DF sd[3], sdA[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      sd[k] = DF{__ldcg(rec + 18 + 2 * k), __ldcg(rec + 19 + 2 * k)};
+      sd[k] = DF{rec[18 + 2 * k], rec[19 + 2 * k]};
       sdA[k] = df_mul(sd[k], inv);
-      mu[k] = df_add_f(sdA[k], __ldcg(rec + DFREC_SHIFT + k));
+      mu[k] = df_add_f(sdA[k], rec[DFREC_SHIFT + k]);
     }
-    const DF g = DF{__ldcg(rec + 24), __ldcg(rec + 25)};
+    const DF g = DF{rec[24], rec[25]};
     ga = df_sub(g, df_add(df_add(df_mul(sdA[0], sd[0]), df_mul(sdA[1], sd[1])), df_mul(sdA[2], sd[2])));
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      const DF bs = DF{ri->sum_hi[k], ri->sum_lo[k]};
 #pragma unroll
-      for (int i = 0; i < 3; ++i) m[3 * i + k] = df_sub(m[3 * i + k], df_mul(sdA[i], bs));
+      for (int i = 0; i < 3; ++i) m[3 * i + k] = df_sub(m[3 * i + k], df_mul(sdA[i], rv.sum[k]));
     }
-    gb = DF{ri->g_hi, ri->g_lo};
+    gb = rv.g;
     if (a.out_centroid)
       for (int k = 0; k < 3; ++k) a.out_centroid[3 * f + k] = __fadd_rn(mu[k].hi, mu[k].lo);
     if (a.out_trace) a.out_trace[f] = __fadd_rn(ga.hi, ga.lo);
@@ -481,9 +491,7 @@ __device__ __forceinline__ void finish_frame_df(const float* rec, int64_t f, con
   const float scale = __fmul_rn(__fadd_rn(ga.hi, gb.hi), 0.5f * inv.hi);
   if (msd * (float)A < 0.01f * scale * scale && A > 0) {
     RefineEntry e;
-    double md[9];
-    for (int i = 0; i < 9; ++i) md[i] = df_to_double(m[i]);
-    qcp_rotation_refine(md, df_to_double(lam), e.rot);
+    qcp_rotation_refine_dfm(m, lam, e.rot);
     e.frame = f;
     for (int k = 0; k < 3; ++k) {
       e.mu_hi[k] = mu[k].hi;
