@@ -43,6 +43,7 @@
 #include "common.cuh"
 #include "qcp.cuh"
 #include "stream.cuh"
+#include "stream_deal.cuh"
 #include "stream_dev.cuh"
 
 namespace gb {
@@ -168,24 +169,18 @@ __device__ __forceinline__ void cursor_unit(Cursor& cur, int64_t u, int32_t S, i
   cur.q1 = (int32_t)(((int64_t)(s + 1) * Q) / S);
 }
 
-// The unit a warp takes at round position v (v = g + k W for warp g): v
-// itself in the full rounds; in the partial last round the highest warps
-// take its units (frames near the start, often the ones closest to the
-// reference and refined, then sit in CTAs that stream one round less), and
-// the others are done (n_units).
+// The unit dealt at round position v (stream_deal.cuh), from the launch's
+// dealing parameters (kernel arguments: no registers held for them).
 __device__ __forceinline__ int64_t place_unit(int64_t v, const StreamArgs& p) {
-  if (v < p.full_units) return v;
-  const int64_t g = v - p.full_units;  // < W
-  return g >= p.part_shift ? v - p.part_shift : p.n_frames * p.splits;
+  return deal_place(v, p.full_units, p.part_shift, p.n_frames * p.splits);
 }
 
-// Advances to the next chunk; returns true when a new unit starts (a unit of
-// the partial round is a warp's last).
+// Advances to the next chunk; returns true when a new unit starts.
 template <int CQ>
 __device__ __forceinline__ bool cursor_next(Cursor& cur, int64_t W, int32_t S, int32_t Q, const StreamArgs& p) {
   cur.c += 1;
   if (cur.q0 + cur.c * CQ >= cur.q1) {
-    cursor_unit<CQ>(cur, cur.unit >= p.full_units ? p.n_frames * p.splits : place_unit(cur.unit + W, p), S, Q);
+    cursor_unit<CQ>(cur, deal_next(cur.unit, W, p.full_units, p.part_shift, p.n_frames * p.splits), S, Q);
     return true;
   }
   return false;
@@ -228,37 +223,13 @@ __device__ __forceinline__ void issue_chunk(const StreamArgs& p, const void* tma
 template <int WARPS>
 constexpr size_t kFinStateBytes = (16 + 8 * (size_t)WARPS + 15) / 16 * 16;
 
-// The CTA's frames with one unit per frame, dealt as place_unit deals them:
-// warp w's k-th frame is b0 + w + k W for k < full, and in the partial round
-// (warps w >= w0 only) full W + b0 + w - shift.  Local index i (the order of
-// the CTA's records and of its finish): w + k WARPS for k < full, then
-// full WARPS + w - w0.
-struct FinSlice {
-  int64_t n;      // frames of this CTA
-  int64_t base;   // first refinement-list entry of this CTA (frames of lower CTAs)
-  int64_t full;   // full rounds
-  int64_t shift;  // W - (frames of the partial round)
-  int64_t w0;     // first warp of this CTA with a frame in the partial round
-};
-
+// This CTA's frames and their local order (stream_deal.cuh).
 __device__ __forceinline__ FinSlice fin_slice(int64_t F, int warps) {
-  const int64_t W = (int64_t)gridDim.x * warps;
-  const int64_t b0 = (int64_t)blockIdx.x * warps;
-  FinSlice s;
-  s.full = F / W;
-  s.shift = W - (F - s.full * W);
-  s.w0 = min((int64_t)warps, max((int64_t)0, s.shift - b0));
-  s.n = s.full * warps + (warps - s.w0);
-  s.base = s.full * warps * (int64_t)blockIdx.x + max((int64_t)0, b0 - s.shift);
-  return s;
+  return fin_slice_of(F, gridDim.x, blockIdx.x, warps);
 }
 
-// Frame of local index i (see FinSlice).
 __device__ __forceinline__ int64_t fin_frame(const FinSlice& s, int64_t i, int warps) {
-  const int64_t W = (int64_t)gridDim.x * warps;
-  const int64_t b0 = (int64_t)blockIdx.x * warps;
-  if (i < s.full * warps) return b0 + (i % warps) + (i / warps) * W;
-  return s.full * W + b0 + (i - s.full * warps + s.w0) - s.shift;
+  return fin_frame_of(s, i, gridDim.x, blockIdx.x, warps);
 }
 
 // Direct residual of one queued frame by the whole CTA (WARPS warps): every
@@ -534,14 +505,8 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
       double* rec = p.sums + unit * SUMS_STRIDE;
       float* recf = reinterpret_cast<float*>(rec);
       if constexpr (FIN) {
-        if (fa.rec_smem) {
-          // local index of the frame (FinSlice): w + k WARPS in the full
-          // rounds, full WARPS + w - w0 in the partial one
-          const int64_t w0 = min((int64_t)WARPS, max((int64_t)0, p.part_shift - (int64_t)blockIdx.x * WARPS));
-          const int64_t li = fin_done < p.full_rounds ? warp + (int64_t)fin_done * WARPS
-                                                      : p.full_rounds * WARPS + warp - w0;
-          recf = fin_rec + li * FREC_FLOATS;
-        }
+        if (fa.rec_smem)
+          recf = fin_rec + fin_local_index(fin_done, warp, p.full_rounds, p.part_shift, blockIdx.x, WARPS) * FREC_FLOATS;
         ++fin_done;
       }
       if constexpr (NV == 1) {
@@ -844,9 +809,7 @@ size_t fin_smem_bytes(int warps) { return align_up(16 + kFinSmemPerWarp * (size_
 // Record slots of the in-kernel finish for the CTA with the most frames
 // (fin_slice: CTA 0), when they are kept in shared memory.
 size_t fin_rec_bytes(int64_t F, int warps, int grid) {
-  const int64_t W = (int64_t)grid * warps;
-  const int64_t n = (F / W) * warps + std::min<int64_t>(warps, F % W);
-  return (size_t)n * FREC_FLOATS * sizeof(float);
+  return (size_t)fin_max_frames(F, grid, warps) * FREC_FLOATS * sizeof(float);
 }
 
 size_t stream_smem_bytes(const StreamCfg& c, int32_t Ap, bool use_ref, bool fin = false, size_t rec_bytes = 0) {
@@ -1009,10 +972,10 @@ int launch_stream(int layout, int mode, const StreamArgs& args, const StreamCfg&
   a.skip_unit = skip_unit_hook();
   const int grid = sm_count();
   {
-    const int64_t W = (int64_t)grid * c.warps, units = a.n_frames * a.splits;
-    a.full_rounds = units / W;
-    a.full_units = a.full_rounds * W;
-    a.part_shift = W - (units - a.full_units);
+    const Deal d = make_deal(a.n_frames * a.splits, (int64_t)grid * c.warps);
+    a.full_rounds = d.full_rounds;
+    a.full_units = d.full_units;
+    a.part_shift = d.part_shift;
   }
   const bool use_ref = mode != MODE_TRACE;
   const size_t rec_bytes = (fin && fin->rec_smem) ? fin_rec_bytes(a.n_frames, c.warps, sm_count()) : 0;

@@ -54,11 +54,8 @@ struct StreamArgs {
   uint64_t wait_ns;      // limit of each bounded wait (gbrmsd_set_wait_limit_ns)
   int64_t skip_unit;     // failure-detection test hook: the first chunk of this
                          // unit is never issued (-1: off)
-  // Units are dealt to the W = grid x warps warps in rounds (warp g takes
-  // g, g + W, ...); the partial last round goes to the highest warps: warp
-  // g >= part_shift takes unit full_units + g - part_shift.  Set by the
-  // launcher: full_rounds = units / W, full_units = full_rounds * W,
-  // part_shift = W - (units - full_units).
+  // Dealing of the units to the warps (stream_deal.cuh, make_deal), set by
+  // the launcher.
   int64_t full_units;
   int64_t part_shift;
   int64_t full_rounds;
