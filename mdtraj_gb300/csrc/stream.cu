@@ -352,18 +352,27 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
   unsigned char* stages = smem + ref_al + (size_t)warp * NSTAGE * STAGE_BYTES;
   uint64_t* bars =
       reinterpret_cast<uint64_t*>(smem + ref_al + (size_t)WARPS * NSTAGE * STAGE_BYTES) + warp * NSTAGE;
+  // the reference's copy into shared memory completes on its own barrier,
+  // after the warps' stage barriers (16 bytes reserved)
+  uint64_t* ref_bar = reinterpret_cast<uint64_t*>(smem + ref_al + (size_t)WARPS * NSTAGE * (STAGE_BYTES + 8));
   // FIN: refinement entries the CTA's finish queued, then the CTA-wide
   // refinement's per-warp partial sums (16-byte aligned)
-  int* fin_nref = reinterpret_cast<int*>(smem + ref_al + (size_t)WARPS * NSTAGE * (STAGE_BYTES + 8));
+  int* fin_nref = reinterpret_cast<int*>(reinterpret_cast<unsigned char*>(ref_bar) + 16);
   CF* fin_part = reinterpret_cast<CF*>(fin_nref + 4);
   float* fin_rec = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(fin_nref) + kFinStateBytes<WARPS>);
   int32_t fin_done = 0;  // frames this warp has recorded
 
+  // The reference goes to shared memory as one bulk copy, issued before any
+  // frame chunk, so that it is in flight while the warps start; every
+  // thread waits for it (bounded) before its first chunk.
   if constexpr (REF_SMEM && USE_REF) {
-    const float4* src = reinterpret_cast<const float4*>(p.ref);
-    float4* dst = reinterpret_cast<float4*>(sref);
-    const int n4 = Ap * 3 / 4;
-    for (int i = threadIdx.x; i < n4; i += blockDim.x) dst[i] = src[i];
+    if (threadIdx.x == 0) {
+      const uint32_t ref_bytes = (uint32_t)Ap * 12u;
+      mbar_init(ref_bar, 1);
+      fence_mbar_init();
+      mbar_arrive_expect_tx(ref_bar, ref_bytes);
+      bulk_g2s(sref, p.ref, ref_bytes, ref_bar);
+    }
   }
   if (lane == 0) {
     for (int s = 0; s < NSTAGE; ++s) mbar_init(&bars[s], 1);
@@ -398,13 +407,14 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
   uint32_t phases = 0;
   int slot = 0;
   bool failed = false;
+  if constexpr (REF_SMEM && USE_REF) failed = !mbar_wait_timed(ref_bar, 0u, p.err, p.wait_ns);
   CF acc2[NV];
   float acc1[NV];
   int pending = 0;  // quads per lane in acc1 since the last fold
   float shift[3] = {0.f, 0.f, 0.f};
 
 #pragma unroll 1
-  while (cc.unit < n_units) {
+  while (!failed && cc.unit < n_units) {
     const bool unit_start = (cc.c == 0);
     if (unit_start) {
 #pragma unroll
@@ -568,6 +578,8 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
     // that timed out included, so that no copy is left in flight into shared
     // memory when the CTA exits; a stage whose copy never arrives costs one
     // more bounded wait and does not stop the others from being drained.
+    // The same for the reference's copy (at once when it has landed).
+    if constexpr (REF_SMEM && USE_REF) mbar_wait_timed(ref_bar, 0u, nullptr, p.wait_ns);
     const int64_t outstanding = issued - consumed;
     for (int64_t i = 0; i < outstanding; ++i) {
       mbar_wait_timed(&bars[slot], (phases >> slot) & 1u, nullptr, p.wait_ns);
@@ -815,7 +827,8 @@ size_t fin_rec_bytes(int64_t F, int warps, int grid) {
 size_t stream_smem_bytes(const StreamCfg& c, int32_t Ap, bool use_ref, bool fin = false, size_t rec_bytes = 0) {
   const size_t ref = (c.ref_smem && use_ref) ? align_up((size_t)Ap * 12, 128) : 0;
   const size_t fin_state = fin ? fin_smem_bytes(c.warps) + rec_bytes : 0;
-  return ref + (size_t)c.warps * c.nstage * c.cq * 48 + (size_t)c.warps * c.nstage * 8 + fin_state;
+  // stages, their barriers, the reference copy's barrier (16 bytes)
+  return ref + (size_t)c.warps * c.nstage * c.cq * 48 + (size_t)c.warps * c.nstage * 8 + 16 + fin_state;
 }
 
 // The in-kernel finish keeps its records in shared memory when the largest
@@ -978,6 +991,8 @@ int launch_stream(int layout, int mode, const StreamArgs& args, const StreamCfg&
     a.part_shift = d.part_shift;
   }
   const bool use_ref = mode != MODE_TRACE;
+  // bulk copies need 16-byte aligned sources (the prepared reference)
+  if (use_ref && !aligned16(a.ref)) return set_error(GBRMSD_E_INVALID, "reference workspace must be 16-byte aligned");
   const size_t rec_bytes = (fin && fin->rec_smem) ? fin_rec_bytes(a.n_frames, c.warps, sm_count()) : 0;
   const size_t smem = stream_smem_bytes(c, a.n_padded, use_ref, fin != nullptr, rec_bytes);
   alignas(64) CUtensorMap tm;
