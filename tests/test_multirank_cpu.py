@@ -135,6 +135,34 @@ def test_frame_range_covers_frames_once():
         frame_range(10, 2, 2)
 
 
+def test_row_requests_cover_the_upper_triangle_once():
+    """The block partition of allpairs_sharded: over the ranks, every pair
+    i <= j is in exactly one range, no range reaches below the diagonal's
+    block, and each rank's ranges are disjoint block rows."""
+    from mdtraj_gb300.shard import default_block, row_requests, triangle_blocks
+
+    for F in (1, 2, 5, 64, 97, 300, 1001):
+        for world in (1, 2, 3, 5, 8):
+            for block in {default_block(F, world), 1, 7, 64, F}:
+                cover = np.zeros((F, F), int)
+                for r in range(world):
+                    rows = set()
+                    for i0, i1, j0, j1 in row_requests(F, block, r, world):
+                        assert 0 <= i0 < i1 <= F and 0 <= j0 < j1 <= F and i0 <= j0
+                        assert i0 not in rows
+                        rows.add(i0)
+                        cover[i0:i1, j0:j1] += 1
+                iu = np.triu_indices(F)
+                assert np.all(cover[iu] == 1), (F, world, block)
+                assert len(triangle_blocks(F, block)) == (-(-F // block)) * (-(-F // block) + 1) // 2
+    # default_block: at least four blocks per rank, unless blocks are already
+    # one frame wide
+    for F, world in ((20_000, 8), (4000, 3), (10, 16), (3, 2)):
+        b = default_block(F, world)
+        nb = -(-F // b)
+        assert nb * (nb + 1) // 2 >= 4 * world or b == 1, (F, world, b)
+
+
 def _fp64_rows(xyz, requests, precentered, method):
     """FP64 Kabsch RMSD of each range's frame pairs (the oracle), as the
     per-rank scorer of allpairs_sharded."""
