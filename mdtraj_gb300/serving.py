@@ -375,8 +375,7 @@ class RmsdServer:
         err = int(slot.hdr[0])  # copied before the batch's event
         refined = int(slot.hdr[2:].view(torch.int64)[0])
         if err:
-            raise _lib.GbrmsdError(_lib.E_DEVICE, "cross RMSD batch: device error word 0x%x (1 = wait expired, "
-                                                  "4 = refinement list full)" % err)
+            raise _lib.GbrmsdError(_lib.E_DEVICE, "cross RMSD batch: device error word 0x%x (1 = wait expired)" % err)
         done = slot.batch
         t_ev, host_s, nbytes = slot.timeline
         self.batch_log.append({"requests": len(done), "result_bytes": nbytes, "launch_host_ms": host_s * 1e3,
