@@ -6,8 +6,10 @@
 // case prints: lambda (mixed FP32/FP64 solve), lambda (FP64 solve), the
 // upper bound (Ga + Gb) / 2, the QCP msd, whether the finish would refine
 // the frame, the direct residual rmsd with the QCP rotation, lambda from
-// the float-float solve (the one the finish kernels use), and the direct
-// residual rmsd with the refinement pass's FP32 rotation.
+// the float-float solve (the one the finish kernels use), the direct
+// residual rmsd with the refinement pass's FP32 rotation, and the same with
+// the in-kernel finish's rotation from float-pair M and lambda
+// (qcp_rotation_refine_dfm).
 #include <cmath>
 #include <cstdio>
 
@@ -83,8 +85,29 @@ int main() {
         s2 += r * r;
       }
     }
-    std::printf("%.17g %.17g %.17g %.17g %d %.17g %.17g %.17g\n", lam, lam64, 0.5 * (ga + gb), msd, refine,
-                std::sqrt(s / A), lamdf, std::sqrt(s2 / A));
+    // the in-kernel finish's refinement rotation, from float-pair M and lambda
+    DF mdf[9];
+    for (int i = 0; i < 9; ++i) mdf[i] = df_from_double(m[i]);
+    int it4 = 0;
+    bool sh4 = false;
+    DF lam_pair = qcp_lambda_max_dfm(mdf, df_mul_f(df_add(df_from_double(ga), df_from_double(gb)), 0.5f), &it4, &sh4);
+    if (sh4) lam_pair = df_from_double(qcp_newton_fp64(m, df_to_double(lam_pair)));
+    float rp[9];
+    qcp_rotation_refine_dfm(mdf, lam_pair, rp);
+    double s3 = 0.0;
+    for (int k = 0; k < A; ++k) {
+      double x[3], y[3];
+      for (int c = 0; c < 3; ++c) {
+        x[c] = a[k][c] - ma[c];
+        y[c] = b[k][c] - mb[c];
+      }
+      for (int i = 0; i < 3; ++i) {
+        const double r = rp[3 * i] * x[0] + rp[3 * i + 1] * x[1] + rp[3 * i + 2] * x[2] - y[i];
+        s3 += r * r;
+      }
+    }
+    std::printf("%.17g %.17g %.17g %.17g %d %.17g %.17g %.17g %.17g\n", lam, lam64, 0.5 * (ga + gb), msd, refine,
+                std::sqrt(s / A), lamdf, std::sqrt(s2 / A), std::sqrt(s3 / A));
   }
   return 0;
 }

@@ -86,6 +86,7 @@ def test_exact_copies_of_collinear_structures(qcp_bin, kind):
     assert np.abs(lamdf - lam0).max() <= 1e-6 * lam0.max()
     assert _finish_rmsd(res).max() < 1e-5
     assert res[:, 7].max() < 1e-5  # the refinement pass's rotation
+    assert res[:, 8].max() < 1e-5  # the same from float-pair M and lambda (in-kernel finish)
 
 
 def test_refinement_rotation_near_identical_frames(qcp_bin):
@@ -98,6 +99,9 @@ def test_refinement_rotation_near_identical_frames(qcp_bin):
     pairs = [_case("general", rng, s) for s in (0.0, 1e-5, 1e-4, 1e-3) for _ in range(100)]
     res = _run(qcp_bin, pairs)
     np.testing.assert_allclose(res[:, 7], res[:, 5], rtol=0, atol=1e-6)
+    # the in-kernel finish builds the same rotation from float-pair M and
+    # lambda, without FP64
+    np.testing.assert_allclose(res[:, 8], res[:, 5], rtol=0, atol=1e-6)
 
 
 @pytest.mark.parametrize("kind,sigma", [("collinear", 0.01), ("atoms2", 0.05), ("general", 0.1), ("general", 1e-4)])
